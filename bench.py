@@ -1,0 +1,338 @@
+#!/usr/bin/env python
+"""bench.py -- LULESH figure of merit (element-cycles per microsecond) on GB300.
+
+One "step" is one cycle of the reference main loop (TimeIncrement +
+LagrangeLeapFrog, lulesh.cc:2745-2757) over the whole mesh.  The default
+workload is the reference's built-in Sedov problem at s=150 (3,375,000
+elements, 11 regions, balance 1, cost 1), 500 cycles from the initial state,
+FP64.  The state (~2 GB) is larger than the 129 MB L2, so no flush is needed
+between cycles.
+
+    python bench.py [--steps 500] [--warmup 5] [--gpus N] [--impl gb300|reference]
+                    [--nx 150] [--regions 11] [--balance 1] [--cost 1]
+                    [--precision fp64|fp64-fma|mixed]
+
+Prints one JSON line.  `value` is the device-timed rate (CUDA events on the
+handle's stream around exactly K cycles, the state resident in HBM);
+`e2e` is the same metric through the C ABI with host buffers: upload of every
+Domain field from pinned host memory, the K cycles, download of every field.
+`--impl reference` times the reference algorithm on the host cores instead
+(the oracle's C restatement, -O3 OpenMP, all host threads), on the same
+workload.  Under torchrun each rank runs an independent replica of the
+problem on its own GPU (the path does not shard on one box); `value` sums the
+element-cycles of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "elem-cycles/µs (LULESH FOM) on 1 GB300: FP64 vs mixed/batched, err vs FP64"
+UNIT = "elem-cycles/us"
+
+# Compulsory HBM bytes per element per cycle of the persistent state each
+# kernel must read or write (FP64 values, int32 indices; node quantities
+# scaled by N/E).  Per-corner scratch and per-cycle temporaries are
+# implementation traffic and not counted.
+#   k_forces:     nodelist 32 + x,y,z,xd,yd,zd 48*N/E + p,q,v,volo,ss,elemMass 48
+#   k_nodes:      read x..zd, nodalMass 56*N/E, write x..zd 48*N/E (+ the
+#                 accessor fields fx..zdd 48*N/E the reference keeps)
+#   k_kinematics: nodelist 32 + x..zd 48*N/E + volo, v 16 + writes vnew,
+#                 delv, arealg, vdov 32
+#   k_material:   lxim..lzetap 24, elemBC 4, region order 4, e,p,q,v,volo,
+#                 ss,elemMass 56 read; e,p,q,v,ss 40 written
+# The whole cycle's compulsory figure is 160 + 104*N/E bytes.
+def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
+    return {
+        "k_forces": 32 + 48 * n_over_e + 48,
+        "k_nodes": (56 + 48 + 48) * n_over_e,
+        "k_kinematics": 32 + 48 * n_over_e + 16 + 32,
+        "k_material": 24 + 4 + 4 + 56 + 40,
+    }.get(kernel, 160 + 104 * n_over_e)
+
+
+# FP64 thread-instructions (DADD + DMUL + DFMA) per element per launch,
+# from an ncu capture of each kernel (profiles/); None where not measured.
+FP64_INST_PER_ELEM = {
+    "fp64": {},
+    "fp64-fma": {},
+}
+
+
+def _peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict | None:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        return dist, ws, rank, local
+    return None, 1, 0, 0
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _workload(a) -> dict:
+    return {"workload": f"Sedov blast, s={a.nx} ({a.nx ** 3} elements, {(a.nx + 1) ** 3} nodes), "
+                        f"{a.regions} regions, balance {a.balance}, cost {a.cost}, "
+                        f"{a.steps} cycles from the initial state, {a.precision}",
+            "nx": a.nx, "regions": a.regions, "balance": a.balance, "cost": a.cost,
+            "cycles": a.steps, "precision": a.precision,
+            "l2": "inputs larger than L2 (resident state ~%.1f GB)" % (
+                (a.nx + 1) ** 3 * 13 * 8 / 1e9 + a.nx ** 3 * (19 * 8 + 17 * 4 + 48 * 8) / 1e9),
+            "parallelism": "replicas"}
+
+
+def cpu_reference_rate(a, budget_s: float, warmup: int, max_cycles: int) -> dict:
+    """Time the reference algorithm (oracle C restatement, OpenMP) on the host."""
+    from oracle import oracle
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    o = oracle.OracleDomain(a.nx, a.regions, a.balance, a.cost, fast=True)
+    setup = time.perf_counter() - t0
+    if warmup:
+        o.step(warmup)
+    E = a.nx ** 3
+    done, t = 0, 0.0
+    while done < max_cycles and t < budget_s:
+        t1 = time.perf_counter()
+        st = o.step(1)
+        t += time.perf_counter() - t1
+        if st:
+            break
+        done += 1
+    o.close()
+    return {"value": E * done / (t * 1e6) if t > 0 else 0.0, "unit": UNIT, "cores": threads,
+            "kind": "port",
+            "sample": f"{done} cycles of s={a.nx} r={a.regions} b={a.balance} c={a.cost} "
+                      f"after {warmup} warm-up cycles ({t:.1f} s timed, set-up {setup:.1f} s "
+                      f"untimed); oracle C restatement -O3 -fopenmp, {threads} threads"}
+
+
+def run_reference(a):
+    dist, ws, rank, local = _dist()
+    if rank != 0:
+        return
+    base = cpu_reference_rate(a, budget_s=float(os.environ.get("LG_REF_BUDGET_S", "120")),
+                              warmup=min(a.warmup, 2), max_cycles=a.steps)
+    line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": ws,
+            "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": (a.nx ** 3 / base["value"] / 1e3) if base["value"] else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: the reference's built-in Sedov problem set-up",
+            "config": _workload(a), "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(a):
+    dist, ws, rank, local = _dist()
+    import numpy as np
+    import lulesh_gb300 as lg
+    try:
+        import torch
+        sync = torch.cuda.synchronize if torch.cuda.is_available() else (lambda: None)
+    except ImportError:
+        torch, sync = None, (lambda: None)
+
+    E, N = a.nx ** 3, (a.nx + 1) ** 3
+    d = lg.Domain(a.nx, a.regions, a.balance, a.cost, its=10 ** 9, precision=a.precision,
+                  device=local)
+    # warm-up cycles, then back to the initial state
+    if a.warmup:
+        d.step(a.warmup)
+    d.reset()
+
+    # device-timed region: exactly K cycles
+    launches0 = d.scalar("launches")
+    _barrier(dist)
+    sync()
+    with ClockSampler(local) as clk:
+        st, ms = d.step_timed(a.steps)
+        sync()
+        _barrier(dist)
+    launches = int(d.scalar("launches") - launches0)
+    if st != 0:
+        raise SystemExit(f"run failed with status {st}")
+    ms_max = _max_over_ranks(dist, ms)
+    value = ws * E * a.steps / (ms_max * 1e3)
+    verify = d.verify()
+
+    # per-kernel device times over a profiled pass of the same cycles
+    d.reset()
+    prof_cycles = min(a.steps, 20)
+    prof = d.profile(prof_cycles)
+    total = sum(prof.values())
+    dom = max(prof, key=prof.get)
+    avg_ms = prof[dom] / prof_cycles
+    peaks = _peaks()
+    ab = alg_bytes_per_elem(dom, N / E) * E
+    achieved = ab / (avg_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": dom,
+                "peak_source": peaks["src"], "alg_bytes_per_launch": ab,
+                "kernel_ms_per_launch": avg_ms,
+                "kernel_share": {k: v / total for k, v in prof.items()}}
+    # FP64 pipe roofline (the bound of this path)
+    fp64_peak = lg.measure_pipe("fma")
+    per_elem = FP64_INST_PER_ELEM.get(a.precision, {}).get(dom)
+    roof64 = {"bound": "fp64_pipe", "peak_ginst_per_s": fp64_peak, "unit": "G FP64 inst/s",
+              "kernel": dom}
+    if per_elem:
+        ach = per_elem * E / (avg_ms * 1e-3) / 1e9
+        roof64.update({"achieved": ach, "frac": ach / fp64_peak,
+                       "inst_per_elem": per_elem})
+
+    # end to end through the C ABI with host buffers
+    fields = lg.NODE_FIELDS + lg.ELEM_FIELDS
+    if torch is not None and torch.cuda.is_available():
+        host = {f: torch.empty(d.field_info(f)[0], dtype=torch.float64,
+                               pin_memory=True).numpy() for f in fields}
+    else:
+        host = {f: np.empty(d.field_info(f)[0]) for f in fields}
+    d.reset()
+    for f in fields:
+        d.field(f, out=host[f])
+    h2d = sum(host[f].nbytes for f in fields)
+    _barrier(dist)
+    t0 = time.perf_counter()
+    for f in fields:
+        d.set_field(f, host[f])
+    st2 = d.step(a.steps)
+    for f in fields:
+        d.field(f, out=host[f])
+    t_e2e = time.perf_counter() - t0
+    _barrier(dist)
+    t_e2e = _max_over_ranks(dist, t_e2e)
+    e2e = {"value": ws * E * a.steps / (t_e2e * 1e6), "unit": UNIT,
+           "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": h2d / a.steps,
+           "status": st2}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if a.precision != "mixed" else "f64+f32",
+            "data": "synthetic: the reference's built-in Sedov problem set-up",
+            "config": _workload(a), "e2e": e2e, "gpu_launches": launches,
+            "roofline": roofline, "roofline_fp64": roof64, "clocks": clk.summary(),
+            "origin_energy": verify["origin_energy"]}
+    if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_reference_rate(
+            a, budget_s=float(os.environ.get("LG_CPU_BUDGET_S", "15")), warmup=1,
+            max_cycles=a.steps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=500)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--nx", type=int, default=150)
+    p.add_argument("--regions", type=int, default=11)
+    p.add_argument("--balance", type=int, default=1)
+    p.add_argument("--cost", type=int, default=1)
+    p.add_argument("--precision", default="fp64", choices=["fp64", "fp64-fma", "mixed"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    a = p.parse_args()
+    if a.warmup < 0 or a.steps < 1:
+        p.error("need --steps >= 1 and --warmup >= 0")
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gpu(a)
+
+
+if __name__ == "__main__":
+    main()

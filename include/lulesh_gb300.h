@@ -1,0 +1,151 @@
+/*
+ * lulesh_gb300.h -- C ABI of the GB300 LULESH Lagrange leap-frog path.
+ *
+ * The reference exposes its hot path as two file-static C++ functions that
+ * mutate a host-side Domain in place and are driven by main():
+ *   TimeIncrement(Domain&)        lulesh.cc:166
+ *   LagrangeLeapFrog(Domain&)     lulesh.cc:2601
+ *   main loop                     lulesh.cc:2745-2757
+ *   Domain accessors              lulesh.h:263-429
+ *   Domain::Domain (problem set-up) lulesh-init.cc:16-194
+ *   VerifyAndWriteFinalOutput     lulesh-util.cc:175-230
+ * and it reports errors by exit(VolumeError = -1) / exit(QStopError = -2)
+ * (lulesh.h:42).  This header replaces that surface with a handle API over a
+ * device-resident Domain.  All pointers are plain host pointers; no CUDA or
+ * PyTorch types appear in the signatures.
+ *
+ * Status codes (every entry point returns one):
+ *    0  LG_OK
+ *   -1  LG_VOLUME_ERROR   (reference exit(VolumeError))
+ *   -2  LG_QSTOP_ERROR    (reference exit(QStopError))
+ *   >0  API / CUDA errors, see lg_status; lg_last_error() has the text.
+ *
+ * Threading: one handle per host thread; each handle owns one CUDA stream.
+ * Ownership: device memory belongs to the handle; host buffers passed to the
+ * get/set calls belong to the caller and are not retained.
+ */
+#ifndef LULESH_GB300_H
+#define LULESH_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lg_domain lg_domain;
+
+enum lg_status {
+    LG_OK = 0,
+    LG_VOLUME_ERROR = -1,
+    LG_QSTOP_ERROR = -2,
+    LG_ERR_INVALID = 1,  /* bad argument or unknown name */
+    LG_ERR_CUDA = 2,     /* CUDA runtime failure */
+    LG_ERR_NOMEM = 3,    /* device or host allocation failed */
+    LG_ERR_STATE = 4     /* handle is in an error state from an earlier call */
+};
+
+enum lg_precision {
+    LG_FP64 = 0,  /* every operation in IEEE double, no FMA contraction */
+    LG_FP64_FMA = 1, /* FP64 with fused multiply-add contraction */
+    LG_MIXED = 2  /* FP32 stress/hourglass/kinematics/Q, FP64 state, EOS and dt */
+};
+
+enum lg_dtype { LG_F64 = 0, LG_I32 = 1 };
+
+/* Command-line options of the reference (lulesh.h:599-609, defaults
+ * lulesh.cc:2682-2690) plus the device-path choices. */
+typedef struct lg_opts {
+    int nx;        /* -s  edge elements (default 30) */
+    int numReg;    /* -r  regions (default 11) */
+    int balance;   /* -b  region balance (default 1) */
+    int cost;      /* -c  extra EOS cost (default 1) */
+    int its;       /* -i  cycle limit (default 9999999) */
+    int precision; /* enum lg_precision (default LG_FP64) */
+    double hgcoef; /* hourglass coefficient, reference constant 3.0 (lulesh-init.cc:25) */
+    double einit_factor; /* factor on the deposited origin energy (default 1.0) */
+    int device;    /* CUDA device ordinal (default 0) */
+} lg_opts;
+
+/* Fill *opts with the reference defaults. */
+void lg_default_opts(lg_opts *opts);
+
+/* Build the Sedov problem exactly as Domain::Domain (lulesh-init.cc:16-194)
+ * on the host and upload it.  *out receives the handle. */
+int lg_create(const lg_opts *opts, lg_domain **out);
+
+void lg_destroy(lg_domain *d);
+
+/* Run at most ncycles iterations of the reference main loop
+ * (lulesh.cc:2745-2757): while (time < stoptime && cycle < its)
+ * { TimeIncrement; LagrangeLeapFrog; }.  Blocks until done.  Returns the
+ * status of the run (0, -1 or -2, or an API error). */
+int lg_step(lg_domain *d, int ncycles);
+
+/* lg_step until time >= stoptime or cycle >= its. */
+int lg_run(lg_domain *d);
+
+/* Same as lg_step, and reports the device time of the cycles in *ms (CUDA
+ * events on the handle's stream). */
+int lg_step_timed(lg_domain *d, int ncycles, double *ms);
+
+/* One piece of the cycle, for phase-level checks (same numbering as the
+ * oracle): 0 TimeIncrement, 1 LagrangeNodal, 2 LagrangeElements,
+ * 3 CalcTimeConstraintsForElems (lulesh.cc:166, 1224, 2432, 2577). */
+int lg_phase(lg_domain *d, int phase);
+
+/* Field access by Domain accessor name (lulesh.h:263-367).  Double fields:
+ * x y z xd yd zd xdd ydd zdd fx fy fz nodalMass e p q ql qq v volo vnew delv
+ * vdov arealg ss elemMass delx_xi delx_eta delx_zeta delv_xi delv_eta
+ * delv_zeta.  Integer fields: nodelist lxim lxip letam letap lzetam lzetap
+ * elemBC regNumList regElemSize symmX symmY symmZ nodeElemStart
+ * nodeElemCornerList.  n is the element count of dst/src and must equal the
+ * field length.  Setting nodelist rebuilds the corner list; setting
+ * regNumList rebuilds the region sets. */
+int lg_field_info(lg_domain *d, const char *name, size_t *count, int *dtype);
+int lg_get_field(lg_domain *d, const char *name, void *dst, size_t n);
+int lg_set_field(lg_domain *d, const char *name, const void *src, size_t n);
+
+/* Scalars (lulesh.h:377-429): time deltatime dtcourant dthydro stoptime
+ * dtmax dtfixed deltatimemultlb deltatimemultub hgcoef cycle its numElem
+ * numNode numReg sizeX cost status launches.  launches counts the kernels
+ * this handle has queued.  Constants are read-only except hgcoef. */
+int lg_get_scalar(lg_domain *d, const char *name, double *value);
+int lg_set_scalar(lg_domain *d, const char *name, double value);
+
+/* EOS repetition count of region r (lulesh.cc:2390-2400). */
+int lg_region_rep(lg_domain *d, int r, int *rep);
+
+/* Write the reference end-of-run report (lulesh-util.cc:175-230) for the
+ * current state into buf (NUL-terminated, truncated to buflen). */
+int lg_report(lg_domain *d, double elapsed_seconds, char *buf, size_t buflen);
+
+/* Origin energy and plane-0 symmetry deltas (lulesh-util.cc:197-212),
+ * computed on the device: out[0]=e(0), out[1]=MaxAbsDiff,
+ * out[2]=TotalAbsDiff, out[3]=MaxRelDiff. */
+int lg_verify(lg_domain *d, double out[4]);
+
+/* Per-kernel device time of ncycles cycles (one event pair per launch),
+ * without CUDA graphs: ms[i] is the summed time of kernel i and names[i] its
+ * name, for i < *nkernels (capacity on input, count on output). */
+int lg_profile(lg_domain *d, int ncycles, double *ms, const char **names, int *nkernels);
+
+/* Restore the state built by lg_create (all fields, time-step state and
+ * cycle count), so a problem can be rerun without rebuilding it.  Fields set
+ * with lg_set_field are not part of that state and are overwritten. */
+int lg_reset(lg_domain *d);
+
+/* Issue-rate microbenchmark of one arithmetic pipe on the current device:
+ * op 0 = fused multiply-add, 1 = add, 2 = multiply; fp32 != 0 selects FP32,
+ * else FP64.  *ginst_per_s receives thread-instructions per second / 1e9.
+ * The FP64 leap-frog path is bound by this rate, not by HBM bandwidth. */
+int lg_measure_pipe(int op, int fp32, double *ginst_per_s);
+
+/* Human-readable description of the most recent error on this thread. */
+const char *lg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

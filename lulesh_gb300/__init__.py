@@ -1,0 +1,286 @@
+"""lulesh_gb300 -- the LULESH Lagrange leap-frog timestep on one GB300.
+
+Python mirror of the reference's Domain surface (lulesh.h:148-595) over the C
+ABI in include/lulesh_gb300.h.  Every compute call runs the native CUDA
+library ``lib/liblulesh_gb300.so``; there is no CPU fallback, and importing a
+``Domain`` without the built library raises.
+
+    from lulesh_gb300 import Domain
+    d = Domain(nx=30, numReg=11, balance=1, cost=1, its=100)
+    d.run()                      # the reference main loop on the GPU
+    print(d.report(elapsed))     # VerifyAndWriteFinalOutput text
+    e = d.field("e")             # numpy copy of an accessor array
+
+Errors the reference turns into exit(-1)/exit(-2) (lulesh.h:42) are returned
+as status codes by ``step``/``run`` (or raised as VolumeError/QStopError with
+``check=True``); API and CUDA failures raise LuleshError.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["Domain", "LuleshError", "VolumeError", "QStopError", "library_path", "load",
+           "FP64", "FP64_FMA", "MIXED", "NODE_FIELDS", "ELEM_FIELDS", "measure_pipe"]
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_PKG, "lib", "liblulesh_gb300.so")
+
+FP64, FP64_FMA, MIXED = 0, 1, 2
+_PRECISION = {"fp64": FP64, "fp64-fma": FP64_FMA, "fp64_fma": FP64_FMA, "mixed": MIXED}
+
+NODE_FIELDS = ["x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy", "fz",
+               "nodalMass"]
+ELEM_FIELDS = ["e", "p", "q", "ql", "qq", "v", "volo", "vnew", "delv", "vdov", "arealg",
+               "ss", "elemMass"]
+
+
+class LuleshError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class VolumeError(LuleshError):
+    """The reference's exit(VolumeError): a non-positive element volume."""
+
+
+class QStopError(LuleshError):
+    """The reference's exit(QStopError): artificial viscosity above qstop."""
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("numReg", ctypes.c_int), ("balance", ctypes.c_int),
+                ("cost", ctypes.c_int), ("its", ctypes.c_int), ("precision", ctypes.c_int),
+                ("hgcoef", ctypes.c_double), ("einit_factor", ctypes.c_double),
+                ("device", ctypes.c_int)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise ImportError(
+            f"{_LIB_PATH} is missing: build it with `python -m lulesh_gb300.build` "
+            "(or __graft_entry__.build()); there is no CPU fallback")
+    lib = ctypes.CDLL(_LIB_PATH)
+    H = ctypes.c_void_p
+    lib.lg_default_opts.argtypes = [ctypes.POINTER(_Opts)]
+    lib.lg_create.argtypes = [ctypes.POINTER(_Opts), ctypes.POINTER(H)]
+    lib.lg_destroy.argtypes = [H]
+    lib.lg_step.argtypes = [H, ctypes.c_int]
+    lib.lg_run.argtypes = [H]
+    lib.lg_step_timed.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.lg_phase.argtypes = [H, ctypes.c_int]
+    lib.lg_field_info.argtypes = [H, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t),
+                                  ctypes.POINTER(ctypes.c_int)]
+    lib.lg_get_field.argtypes = [H, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t]
+    lib.lg_set_field.argtypes = [H, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t]
+    lib.lg_get_scalar.argtypes = [H, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
+    lib.lg_set_scalar.argtypes = [H, ctypes.c_char_p, ctypes.c_double]
+    lib.lg_region_rep.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.lg_report.argtypes = [H, ctypes.c_double, ctypes.c_char_p, ctypes.c_size_t]
+    lib.lg_verify.argtypes = [H, ctypes.POINTER(ctypes.c_double)]
+    lib.lg_profile.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_int)]
+    lib.lg_reset.argtypes = [H]
+    lib.lg_measure_pipe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.lg_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def measure_pipe(op: str = "fma", fp32: bool = False) -> float:
+    """Measured issue rate of one arithmetic pipe, in 1e9 thread-instructions/s."""
+    lib = load()
+    v = ctypes.c_double()
+    st = lib.lg_measure_pipe({"fma": 0, "add": 1, "mul": 2}[op], int(fp32), ctypes.byref(v))
+    if st:
+        _raise(st, lib)
+    return v.value
+
+
+def _raise(code: int, lib) -> None:
+    msg = (lib.lg_last_error() or b"").decode()
+    if code == -1:
+        raise VolumeError(code, msg or "VolumeError")
+    if code == -2:
+        raise QStopError(code, msg or "QStopError")
+    raise LuleshError(code, msg)
+
+
+class Domain:
+    """A Sedov problem resident on the GPU, driven through the C ABI.
+
+    Constructor arguments are the reference's -s -r -b -c -i options
+    (lulesh.cc:2682-2690 defaults) plus the device-path choices.
+    """
+
+    def __init__(self, nx: int = 30, numReg: int = 11, balance: int = 1, cost: int = 1,
+                 its: int = 9999999, precision: str | int = "fp64", hgcoef: float = 3.0,
+                 einit_factor: float = 1.0, device: int = 0):
+        lib = load()
+        self._lib = lib
+        o = _Opts()
+        lib.lg_default_opts(ctypes.byref(o))
+        o.nx, o.numReg, o.balance, o.cost, o.its = nx, numReg, balance, cost, its
+        o.precision = _PRECISION[precision] if isinstance(precision, str) else int(precision)
+        o.hgcoef, o.einit_factor, o.device = hgcoef, einit_factor, device
+        h = ctypes.c_void_p()
+        st = lib.lg_create(ctypes.byref(o), ctypes.byref(h))
+        if st:
+            _raise(st, lib)
+        self._h = h
+        self.nx = nx
+        self.numElem = nx ** 3
+        self.numNode = (nx + 1) ** 3
+
+    # lifetime -------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # time stepping -------------------------------------------------------
+    def _status(self, st: int, check: bool) -> int:
+        if st > 0 or (check and st < 0):
+            _raise(st, self._lib)
+        return st
+
+    def step(self, ncycles: int = 1, check: bool = False) -> int:
+        """Up to ncycles of TimeIncrement + LagrangeLeapFrog; returns 0/-1/-2."""
+        return self._status(self._lib.lg_step(self._h, int(ncycles)), check)
+
+    def run(self, check: bool = False) -> int:
+        """The reference main loop until stoptime or its (lulesh.cc:2745)."""
+        return self._status(self._lib.lg_run(self._h), check)
+
+    def step_timed(self, ncycles: int) -> tuple[int, float]:
+        ms = ctypes.c_double()
+        st = self._lib.lg_step_timed(self._h, int(ncycles), ctypes.byref(ms))
+        self._status(st, False)
+        return st, ms.value
+
+    def reset(self) -> None:
+        """Restore the state built at creation (lg_reset)."""
+        st = self._lib.lg_reset(self._h)
+        if st:
+            _raise(st, self._lib)
+
+    def phase(self, which: int) -> int:
+        return self._status(self._lib.lg_phase(self._h, int(which)), False)
+
+    def profile(self, ncycles: int) -> dict:
+        cap = 16
+        ms = (ctypes.c_double * cap)()
+        names = (ctypes.c_char_p * cap)()
+        n = ctypes.c_int(cap)
+        st = self._lib.lg_profile(self._h, int(ncycles), ms, names, ctypes.byref(n))
+        self._status(st, False)
+        return {names[i].decode(): ms[i] for i in range(n.value)}
+
+    # fields --------------------------------------------------------------
+    def field_info(self, name: str) -> tuple[int, np.dtype]:
+        n = ctypes.c_size_t()
+        dt = ctypes.c_int()
+        st = self._lib.lg_field_info(self._h, name.encode(), ctypes.byref(n), ctypes.byref(dt))
+        if st:
+            _raise(st, self._lib)
+        return n.value, (np.float64 if dt.value == 0 else np.int32)
+
+    def field(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+        """Copy of the accessor array `name` (lulesh.h:263-367)."""
+        n, dt = self.field_info(name)
+        if out is None:
+            out = np.empty(n, dtype=dt)
+        if out.dtype != dt or out.size != n or not out.flags.c_contiguous:
+            raise ValueError(f"{name}: need a contiguous {np.dtype(dt)}[{n}] buffer")
+        st = self._lib.lg_get_field(self._h, name.encode(), out.ctypes.data, n)
+        if st:
+            _raise(st, self._lib)
+        return out
+
+    def set_field(self, name: str, values) -> None:
+        n, dt = self.field_info(name)
+        a = np.ascontiguousarray(values, dtype=dt)
+        if a.size != n:
+            raise ValueError(f"{name}: expected {n} entries, got {a.size}")
+        st = self._lib.lg_set_field(self._h, name.encode(), a.ctypes.data, n)
+        if st:
+            _raise(st, self._lib)
+
+    def scalar(self, name: str) -> float:
+        v = ctypes.c_double()
+        st = self._lib.lg_get_scalar(self._h, name.encode(), ctypes.byref(v))
+        if st:
+            _raise(st, self._lib)
+        return v.value
+
+    def set_scalar(self, name: str, value: float) -> None:
+        st = self._lib.lg_set_scalar(self._h, name.encode(), float(value))
+        if st:
+            _raise(st, self._lib)
+
+    @property
+    def cycle(self) -> int:
+        return int(self.scalar("cycle"))
+
+    @property
+    def time(self) -> float:
+        return self.scalar("time")
+
+    @property
+    def deltatime(self) -> float:
+        return self.scalar("deltatime")
+
+    def region_rep(self, r: int) -> int:
+        v = ctypes.c_int()
+        st = self._lib.lg_region_rep(self._h, r, ctypes.byref(v))
+        if st:
+            _raise(st, self._lib)
+        return v.value
+
+    def state(self) -> dict:
+        out = {f: self.field(f) for f in NODE_FIELDS + ELEM_FIELDS}
+        for s in ("time", "deltatime", "dtcourant", "dthydro", "cycle"):
+            out[s] = self.scalar(s)
+        return out
+
+    # report --------------------------------------------------------------
+    def verify(self) -> dict:
+        v = (ctypes.c_double * 4)()
+        st = self._lib.lg_verify(self._h, v)
+        if st:
+            _raise(st, self._lib)
+        return {"origin_energy": v[0], "MaxAbsDiff": v[1], "TotalAbsDiff": v[2],
+                "MaxRelDiff": v[3]}
+
+    def report(self, elapsed: float) -> str:
+        buf = ctypes.create_string_buffer(8192)
+        st = self._lib.lg_report(self._h, float(elapsed), buf, len(buf))
+        if st:
+            _raise(st, self._lib)
+        return buf.value.decode()

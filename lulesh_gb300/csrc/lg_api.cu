@@ -1,0 +1,803 @@
+// lg_api.cu -- the C ABI (include/lulesh_gb300.h): handle, device memory,
+// upload/download, the cycle loop under CUDA graphs, and the report.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lg_device.h"
+#include "lg_kernelset.h"
+#include "lg_problem.h"
+#include "lulesh_gb300.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define LG_CUDA(call)                                                                   \
+    do {                                                                                \
+        cudaError_t err_ = (call);                                                      \
+        if (err_ != cudaSuccess)                                                        \
+            return set_error(LG_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(err_), \
+                             __FILE__, __LINE__);                                       \
+    } while (0)
+
+constexpr size_t kAlign = 256;
+size_t align_up(size_t v) { return (v + kAlign - 1) & ~(kAlign - 1); }
+
+// Sub-allocations of the single device arena.
+struct Layout {
+    size_t total = 0;
+    template <typename T>
+    size_t add(size_t count)
+    {
+        const size_t off = total;
+        total = align_up(total + count * sizeof(T));
+        return off;
+    }
+};
+
+}  // namespace
+
+struct lg_domain {
+    lg_opts opts{};
+    lg::Problem prob;  // host mirror: integer fields and the initial state
+    lg::DevState ds{};
+    const lg::KernelSet *ks = nullptr;
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+    cudaStream_t stream = nullptr;
+    lg::Ctl *h_ctl = nullptr;  // pinned host copy of the control block
+    cudaGraphExec_t graph1 = nullptr, graph16 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int its = 9999999;
+    bool host_only = false;  // device < 0: problem set-up only, no GPU
+    long long launches = 0;  // kernels queued by this handle
+};
+
+namespace {
+
+int ensure_device(lg_domain *d)
+{
+    if (d->host_only)
+        return set_error(LG_ERR_STATE, "handle was created host-only (device < 0)");
+    LG_CUDA(cudaSetDevice(d->opts.device));
+    return LG_OK;
+}
+
+void drop_graphs(lg_domain *d)
+{
+    if (d->graph1) cudaGraphExecDestroy(d->graph1);
+    if (d->graph16) cudaGraphExecDestroy(d->graph16);
+    d->graph1 = d->graph16 = nullptr;
+}
+
+lg::Params make_params(const lg::Constants &k)
+{
+    lg::Params p;
+    p.e_cut = k.e_cut; p.p_cut = k.p_cut; p.q_cut = k.q_cut; p.v_cut = k.v_cut;
+    p.u_cut = k.u_cut; p.hgcoef = k.hgcoef; p.ss4o3 = k.ss4o3; p.qstop = k.qstop;
+    p.monoq_max_slope = k.monoq_max_slope; p.monoq_limiter_mult = k.monoq_limiter_mult;
+    p.qlc_monoq = k.qlc_monoq; p.qqc_monoq = k.qqc_monoq; p.qqc = k.qqc;
+    p.eosvmax = k.eosvmax; p.eosvmin = k.eosvmin; p.pmin = k.pmin; p.emin = k.emin;
+    p.dvovmax = k.dvovmax; p.refdens = k.refdens;
+    return p;
+}
+
+template <typename T>
+int upload(lg_domain *d, T *dst, const std::vector<T> &src)
+{
+    if (src.empty()) return LG_OK;
+    LG_CUDA(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice,
+                            d->stream));
+    return LG_OK;
+}
+
+// Kernel-side layouts derived from the integer fields (see lg_device.h).
+int upload_topology(lg_domain *d)
+{
+    const lg::Problem &p = d->prob;
+    const int E = p.numElem, N = p.numNode;
+    std::vector<int> nlT(8 * (size_t)E);
+    for (int e = 0; e < E; ++e)
+        for (int j = 0; j < 8; ++j) nlT[(size_t)j * E + e] = p.nodelist[8 * (size_t)e + j];
+    std::vector<uint8_t> symm(N, 0);
+    for (int n : p.symmX) symm[n] |= 1;
+    for (int n : p.symmY) symm[n] |= 2;
+    for (int n : p.symmZ) symm[n] |= 4;
+    std::vector<int> perm, rep;
+    perm.reserve(E);
+    rep.reserve(E);
+    for (int r = 0; r < p.numReg; ++r) {
+        const int rr = lg::region_rep(r, p.numReg, p.cost);
+        for (int e : p.regElemlist[r]) {
+            perm.push_back(e);
+            rep.push_back(rr);
+        }
+    }
+    if ((int)perm.size() != E) return set_error(LG_ERR_INVALID, "region sets do not cover all elements");
+    int st;
+    if ((st = upload(d, d->ds.nodelist, p.nodelist))) return st;
+    if ((st = upload(d, d->ds.nodelistT, nlT))) return st;
+    if ((st = upload(d, d->ds.symm, symm))) return st;
+    if ((st = upload(d, d->ds.nodeElemStart, p.nodeElemStart))) return st;
+    if ((st = upload(d, d->ds.nodeElemCornerList, p.nodeElemCornerList))) return st;
+    if ((st = upload(d, d->ds.lxim, p.lxim))) return st;
+    if ((st = upload(d, d->ds.lxip, p.lxip))) return st;
+    if ((st = upload(d, d->ds.letam, p.letam))) return st;
+    if ((st = upload(d, d->ds.letap, p.letap))) return st;
+    if ((st = upload(d, d->ds.lzetam, p.lzetam))) return st;
+    if ((st = upload(d, d->ds.lzetap, p.lzetap))) return st;
+    if ((st = upload(d, d->ds.elemBC, p.elemBC))) return st;
+    if ((st = upload(d, d->ds.regNumList, p.regNumList))) return st;
+    if ((st = upload(d, d->ds.regPerm, perm))) return st;
+    if ((st = upload(d, d->ds.regRep, rep))) return st;
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    return LG_OK;
+}
+
+// double fields that live on the device
+bool find_f64(lg_domain *d, const char *name, double **ptr, size_t *count)
+{
+    lg::DevState &s = d->ds;
+    const size_t N = s.N, E = s.E;
+    struct { const char *n; double *p; size_t c; } t[] = {
+        {"x", s.x, N}, {"y", s.y, N}, {"z", s.z, N}, {"xd", s.xd, N}, {"yd", s.yd, N},
+        {"zd", s.zd, N}, {"xdd", s.xdd, N}, {"ydd", s.ydd, N}, {"zdd", s.zdd, N},
+        {"fx", s.fx, N}, {"fy", s.fy, N}, {"fz", s.fz, N}, {"nodalMass", s.nodalMass, N},
+        {"e", s.e, E}, {"p", s.p, E}, {"q", s.q, E}, {"ql", s.ql, E}, {"qq", s.qq, E},
+        {"v", s.v, E}, {"volo", s.volo, E}, {"vnew", s.vnew, E}, {"delv", s.delv, E},
+        {"vdov", s.vdov, E}, {"arealg", s.arealg, E}, {"ss", s.ss, E},
+        {"elemMass", s.elemMass, E}, {"delx_xi", s.delx_xi, E}, {"delx_eta", s.delx_eta, E},
+        {"delx_zeta", s.delx_zeta, E}, {"delv_xi", s.delv_xi, E}, {"delv_eta", s.delv_eta, E},
+        {"delv_zeta", s.delv_zeta, E}};
+    for (auto &f : t)
+        if (!strcmp(f.n, name)) {
+            *ptr = f.p;
+            *count = f.c;
+            return true;
+        }
+    return false;
+}
+
+// double fields of the host mirror (the state built by set-up)
+std::vector<double> *find_f64_host(lg_domain *d, const char *name)
+{
+    lg::Problem &p = d->prob;
+    struct { const char *n; std::vector<double> *v; } t[] = {
+        {"x", &p.x}, {"y", &p.y}, {"z", &p.z}, {"xd", &p.xd}, {"yd", &p.yd}, {"zd", &p.zd},
+        {"xdd", &p.xdd}, {"ydd", &p.ydd}, {"zdd", &p.zdd}, {"fx", &p.fx}, {"fy", &p.fy},
+        {"fz", &p.fz}, {"nodalMass", &p.nodalMass}, {"e", &p.e}, {"p", &p.p}, {"q", &p.q},
+        {"ql", &p.ql}, {"qq", &p.qq}, {"v", &p.v}, {"volo", &p.volo}, {"vnew", &p.vnew},
+        {"delv", &p.delv}, {"vdov", &p.vdov}, {"arealg", &p.arealg}, {"ss", &p.ss},
+        {"elemMass", &p.elemMass}};
+    for (auto &f : t)
+        if (!strcmp(f.n, name)) return f.v;
+    return nullptr;
+}
+
+// integer fields, served from the host mirror
+std::vector<int> *find_i32(lg_domain *d, const char *name)
+{
+    lg::Problem &p = d->prob;
+    struct { const char *n; std::vector<int> *v; } t[] = {
+        {"nodelist", &p.nodelist}, {"lxim", &p.lxim}, {"lxip", &p.lxip},
+        {"letam", &p.letam}, {"letap", &p.letap}, {"lzetam", &p.lzetam},
+        {"lzetap", &p.lzetap}, {"elemBC", &p.elemBC}, {"regNumList", &p.regNumList},
+        {"regElemSize", &p.regElemSize}, {"symmX", &p.symmX}, {"symmY", &p.symmY},
+        {"symmZ", &p.symmZ}, {"nodeElemStart", &p.nodeElemStart},
+        {"nodeElemCornerList", &p.nodeElemCornerList}};
+    for (auto &f : t)
+        if (!strcmp(f.n, name)) return f.v;
+    return nullptr;
+}
+
+int read_ctl(lg_domain *d)
+{
+    LG_CUDA(cudaMemcpyAsync(d->h_ctl, d->ds.ctl, sizeof(lg::Ctl), cudaMemcpyDeviceToHost,
+                            d->stream));
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    return LG_OK;
+}
+
+int write_ctl(lg_domain *d)
+{
+    LG_CUDA(cudaMemcpyAsync(d->ds.ctl, d->h_ctl, sizeof(lg::Ctl), cudaMemcpyHostToDevice,
+                            d->stream));
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    return LG_OK;
+}
+
+void enqueue_cycle(lg_domain *d)
+{
+    d->ks->launch(lg::K_FORCES, d->ds, 0, d->stream);
+    d->ks->launch(lg::K_NODES, d->ds, 0, d->stream);
+    d->ks->launch(lg::K_KINEMATICS, d->ds, 0, d->stream);
+    d->ks->launch(lg::K_MATERIAL, d->ds, 2, d->stream);
+}
+
+int capture(lg_domain *d, int ncycles, cudaGraphExec_t *out)
+{
+    cudaGraph_t g = nullptr;
+    LG_CUDA(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < ncycles; ++i) enqueue_cycle(d);
+    LG_CUDA(cudaStreamEndCapture(d->stream, &g));
+    cudaError_t err = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (err != cudaSuccess)
+        return set_error(LG_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(err));
+    return LG_OK;
+}
+
+int ensure_graphs(lg_domain *d)
+{
+    int st;
+    if (!d->graph1 && (st = capture(d, 1, &d->graph1))) return st;
+    if (!d->graph16 && (st = capture(d, 16, &d->graph16))) return st;
+    return LG_OK;
+}
+
+// Queue ncycles cycles behind a k_begin that evaluates the loop test.
+int enqueue_cycles(lg_domain *d, int ncycles)
+{
+    int st;
+    if ((st = read_ctl(d))) return st;
+    if (d->h_ctl->status != 0) return d->h_ctl->status;
+    const long long limit = std::min<long long>(d->its, (long long)d->h_ctl->cycle + ncycles);
+    const int lim = (int)limit;
+    LG_CUDA(cudaMemcpyAsync(&d->ds.ctl->cycle_limit, &lim, sizeof(int), cudaMemcpyHostToDevice,
+                            d->stream));
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    if ((st = ensure_graphs(d))) return st;
+    d->ks->begin(d->ds.ctl, d->stream);
+    int left = ncycles;
+    while (left >= 16) {
+        LG_CUDA(cudaGraphLaunch(d->graph16, d->stream));
+        left -= 16;
+    }
+    while (left-- > 0) LG_CUDA(cudaGraphLaunch(d->graph1, d->stream));
+    LG_CUDA(cudaGetLastError());
+    d->launches += 1 + 4LL * ncycles;
+    return LG_OK;
+}
+
+// Upload the state built by set-up (fields, topology, time-step state).
+int upload_initial_state(lg_domain *d)
+{
+    lg::Problem &p = d->prob;
+    int st;
+    double *fld;
+    size_t cnt;
+    std::vector<double> *hostf[26] = {&p.x, &p.y, &p.z, &p.xd, &p.yd, &p.zd, &p.xdd, &p.ydd,
+                                      &p.zdd, &p.fx, &p.fy, &p.fz, &p.nodalMass, &p.e, &p.p,
+                                      &p.q, &p.ql, &p.qq, &p.v, &p.volo, &p.vnew, &p.delv,
+                                      &p.vdov, &p.arealg, &p.ss, &p.elemMass};
+    const char *names[26] = {"x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy",
+                             "fz", "nodalMass", "e", "p", "q", "ql", "qq", "v", "volo", "vnew",
+                             "delv", "vdov", "arealg", "ss", "elemMass"};
+    for (int i = 0; i < 26; ++i) {
+        find_f64(d, names[i], &fld, &cnt);
+        if ((st = upload(d, fld, *hostf[i]))) return st;
+    }
+    if ((st = upload_topology(d))) return st;
+
+    lg::Ctl &c = *d->h_ctl;
+    memset(&c, 0, sizeof(c));
+    c.time = p.t.time;
+    c.deltatime = p.t.deltatime;
+    c.dtcourant = p.t.dtcourant;
+    c.dthydro = p.t.dthydro;
+    c.stoptime = p.t.stoptime;
+    c.dtmax = p.t.dtmax;
+    c.dtfixed = p.t.dtfixed;
+    c.dtmultlb = p.t.deltatimemultlb;
+    c.dtmultub = p.t.deltatimemultub;
+    c.cycle = p.t.cycle;
+    c.cycle_limit = 0;
+    return write_ctl(d);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *lg_last_error(void) { return g_last_error.c_str(); }
+
+void lg_default_opts(lg_opts *o)
+{
+    if (!o) return;
+    o->nx = 30;
+    o->numReg = 11;
+    o->balance = 1;
+    o->cost = 1;
+    o->its = 9999999;
+    o->precision = LG_FP64;
+    o->hgcoef = 3.0;
+    o->einit_factor = 1.0;
+    o->device = 0;
+}
+
+int lg_create(const lg_opts *opts, lg_domain **out)
+{
+    if (!opts || !out) return set_error(LG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (opts->nx < 1 || opts->numReg < 1 || opts->its < 0)
+        return set_error(LG_ERR_INVALID, "invalid problem size (nx=%d numReg=%d its=%d)",
+                         opts->nx, opts->numReg, opts->its);
+    if ((long long)opts->nx * opts->nx * opts->nx * 8 > 2147483647LL)
+        return set_error(LG_ERR_INVALID, "nx=%d exceeds the 32-bit corner index range", opts->nx);
+    const lg::KernelSet *ks = nullptr;
+    switch (opts->precision) {
+    case LG_FP64: ks = lg::kernels_fp64_strict(); break;
+    case LG_FP64_FMA: ks = lg::kernels_fp64_fma(); break;
+    default: return set_error(LG_ERR_INVALID, "precision %d not available", opts->precision);
+    }
+    lg_domain *d = new lg_domain();
+    d->opts = *opts;
+    d->its = opts->its;
+    d->ks = ks;
+    d->host_only = opts->device < 0;
+    int st;
+    if (!d->host_only && (st = ensure_device(d))) {
+        delete d;
+        return st;
+    }
+    d->prob = lg::build_sedov(opts->nx, opts->numReg, opts->balance, opts->cost, opts->hgcoef,
+                              opts->einit_factor);
+    lg::Problem &p = d->prob;
+    if (d->host_only) {
+        d->ds.E = p.numElem;
+        d->ds.N = p.numNode;
+        d->ds.prm = make_params(p.k);
+        *out = d;
+        return LG_OK;
+    }
+    const size_t E = p.numElem, N = p.numNode;
+    const int eblocks = (int)((E + 127) / 128);
+
+    Layout L;
+    size_t o_node[13], o_elem[19];
+    for (auto &o : o_node) o = L.add<double>(N);
+    for (auto &o : o_elem) o = L.add<double>(E);
+    const size_t o_corner = L.add<double>(48 * E);
+    const size_t o_nl = L.add<int>(8 * E), o_nlT = L.add<int>(8 * E);
+    size_t o_conn[7];
+    for (auto &o : o_conn) o = L.add<int>(E);
+    const size_t o_regnum = L.add<int>(E), o_perm = L.add<int>(E), o_rep = L.add<int>(E);
+    const size_t o_nes = L.add<int>(N + 1), o_ncl = L.add<int>(8 * E);
+    const size_t o_symm = L.add<uint8_t>(N);
+    const size_t o_part = L.add<double>(2 * (size_t)eblocks);
+    const size_t o_ctl = L.add<lg::Ctl>(1);
+
+    cudaError_t err = cudaMalloc(&d->arena, L.total);
+    if (err != cudaSuccess) {
+        delete d;
+        return set_error(LG_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", L.total, cudaGetErrorString(err));
+    }
+    d->arena_bytes = L.total;
+    char *base = static_cast<char *>(d->arena);
+    lg::DevState &s = d->ds;
+    s.E = (int)E;
+    s.N = (int)N;
+    s.nx = p.nx;
+    s.numReg = p.numReg;
+    double **nodef[13] = {&s.x, &s.y, &s.z, &s.xd, &s.yd, &s.zd, &s.xdd, &s.ydd, &s.zdd,
+                          &s.fx, &s.fy, &s.fz, &s.nodalMass};
+    for (int i = 0; i < 13; ++i) *nodef[i] = reinterpret_cast<double *>(base + o_node[i]);
+    double **elemf[19] = {&s.e, &s.p, &s.q, &s.ql, &s.qq, &s.v, &s.volo, &s.vnew, &s.delv,
+                          &s.vdov, &s.arealg, &s.ss, &s.elemMass, &s.delx_xi, &s.delx_eta,
+                          &s.delx_zeta, &s.delv_xi, &s.delv_eta, &s.delv_zeta};
+    for (int i = 0; i < 19; ++i) *elemf[i] = reinterpret_cast<double *>(base + o_elem[i]);
+    s.corner = reinterpret_cast<double *>(base + o_corner);
+    s.nodelist = reinterpret_cast<int *>(base + o_nl);
+    s.nodelistT = reinterpret_cast<int *>(base + o_nlT);
+    int **conn[7] = {&s.lxim, &s.lxip, &s.letam, &s.letap, &s.lzetam, &s.lzetap, &s.elemBC};
+    for (int i = 0; i < 7; ++i) *conn[i] = reinterpret_cast<int *>(base + o_conn[i]);
+    s.regNumList = reinterpret_cast<int *>(base + o_regnum);
+    s.regPerm = reinterpret_cast<int *>(base + o_perm);
+    s.regRep = reinterpret_cast<int *>(base + o_rep);
+    s.nodeElemStart = reinterpret_cast<int *>(base + o_nes);
+    s.nodeElemCornerList = reinterpret_cast<int *>(base + o_ncl);
+    s.symm = reinterpret_cast<uint8_t *>(base + o_symm);
+    s.dt_partial = reinterpret_cast<double *>(base + o_part);
+    s.dt_blocks = eblocks;
+    s.ctl = reinterpret_cast<lg::Ctl *>(base + o_ctl);
+    s.prm = make_params(p.k);
+
+    auto fail = [&](int code) {
+        lg_destroy(d);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost(&d->h_ctl, sizeof(lg::Ctl)) != cudaSuccess ||
+        cudaEventCreate(&d->ev0) != cudaSuccess || cudaEventCreate(&d->ev1) != cudaSuccess)
+        return fail(set_error(LG_ERR_CUDA, "stream/event/pinned allocation failed"));
+    if (cudaMemsetAsync(d->arena, 0, L.total, d->stream) != cudaSuccess)
+        return fail(set_error(LG_ERR_CUDA, "cudaMemset failed"));
+
+    if ((st = upload_initial_state(d))) return fail(st);
+    *out = d;
+    return LG_OK;
+}
+
+int lg_reset(lg_domain *d)
+{
+    if (!d) return set_error(LG_ERR_INVALID, "null handle");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    return upload_initial_state(d);
+}
+
+void lg_destroy(lg_domain *d)
+{
+    if (!d) return;
+    if (d->host_only) {
+        delete d;
+        return;
+    }
+    cudaSetDevice(d->opts.device);
+    if (d->stream) cudaStreamSynchronize(d->stream);
+    drop_graphs(d);
+    if (d->ev0) cudaEventDestroy(d->ev0);
+    if (d->ev1) cudaEventDestroy(d->ev1);
+    if (d->h_ctl) cudaFreeHost(d->h_ctl);
+    if (d->arena) cudaFree(d->arena);
+    if (d->stream) cudaStreamDestroy(d->stream);
+    delete d;
+}
+
+int lg_step(lg_domain *d, int ncycles)
+{
+    if (!d || ncycles < 0) return set_error(LG_ERR_INVALID, "invalid argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    if (ncycles == 0) return LG_OK;
+    if ((st = enqueue_cycles(d, ncycles))) return st;
+    if ((st = read_ctl(d))) return st;
+    return d->h_ctl->status;
+}
+
+int lg_step_timed(lg_domain *d, int ncycles, double *ms)
+{
+    if (!d || ncycles < 0 || !ms) return set_error(LG_ERR_INVALID, "invalid argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    if ((st = ensure_graphs(d))) return st;
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    // the control-block write of enqueue_cycles happens before ev0
+    if ((st = read_ctl(d))) return st;
+    if (d->h_ctl->status != 0) return d->h_ctl->status;
+    const long long limit = std::min<long long>(d->its, (long long)d->h_ctl->cycle + ncycles);
+    const int lim = (int)limit;
+    LG_CUDA(cudaMemcpyAsync(&d->ds.ctl->cycle_limit, &lim, sizeof(int), cudaMemcpyHostToDevice,
+                            d->stream));
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    LG_CUDA(cudaEventRecord(d->ev0, d->stream));
+    d->ks->begin(d->ds.ctl, d->stream);
+    int left = ncycles;
+    while (left >= 16) {
+        LG_CUDA(cudaGraphLaunch(d->graph16, d->stream));
+        left -= 16;
+    }
+    while (left-- > 0) LG_CUDA(cudaGraphLaunch(d->graph1, d->stream));
+    LG_CUDA(cudaEventRecord(d->ev1, d->stream));
+    d->launches += 1 + 4LL * ncycles;
+    LG_CUDA(cudaEventSynchronize(d->ev1));
+    float f = 0.f;
+    LG_CUDA(cudaEventElapsedTime(&f, d->ev0, d->ev1));
+    *ms = f;
+    if ((st = read_ctl(d))) return st;
+    return d->h_ctl->status;
+}
+
+int lg_run(lg_domain *d)
+{
+    if (!d) return set_error(LG_ERR_INVALID, "null handle");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    if ((st = read_ctl(d))) return st;
+    for (;;) {
+        const lg::Ctl &c = *d->h_ctl;
+        if (c.status) return c.status;
+        if (!(c.time < c.stoptime && c.cycle < d->its)) return LG_OK;
+        // chunks of at most 64 cycles; lg_step leaves h_ctl current
+        const int n = (int)std::min<long long>(64, (long long)d->its - c.cycle);
+        if ((st = lg_step(d, n))) return st;
+    }
+}
+
+int lg_phase(lg_domain *d, int phase)
+{
+    if (!d) return set_error(LG_ERR_INVALID, "null handle");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    switch (phase) {
+    case 0: d->ks->time_increment(d->ds.ctl, d->stream); break;
+    case 1:
+        d->ks->set_active(d->ds.ctl, d->stream);
+        d->ks->launch(lg::K_FORCES, d->ds, 0, d->stream);
+        d->ks->launch(lg::K_NODES, d->ds, 0, d->stream);
+        break;
+    case 2:
+        d->ks->set_active(d->ds.ctl, d->stream);
+        d->ks->launch(lg::K_KINEMATICS, d->ds, 0, d->stream);
+        d->ks->launch(lg::K_MATERIAL, d->ds, 0, d->stream);
+        break;
+    case 3:
+        d->ks->set_active(d->ds.ctl, d->stream);
+        d->ks->launch(lg::K_MATERIAL, d->ds, 1, d->stream);
+        break;
+    default: return set_error(LG_ERR_INVALID, "unknown phase %d", phase);
+    }
+    LG_CUDA(cudaGetLastError());
+    if ((st = read_ctl(d))) return st;
+    return d->h_ctl->status;
+}
+
+int lg_field_info(lg_domain *d, const char *name, size_t *count, int *dtype)
+{
+    if (!d || !name) return set_error(LG_ERR_INVALID, "null argument");
+    double *p;
+    size_t c;
+    if (find_f64(d, name, &p, &c)) {
+        if (count) *count = c;
+        if (dtype) *dtype = LG_F64;
+        return LG_OK;
+    }
+    if (std::vector<int> *v = find_i32(d, name)) {
+        if (count) *count = v->size();
+        if (dtype) *dtype = LG_I32;
+        return LG_OK;
+    }
+    return set_error(LG_ERR_INVALID, "unknown field '%s'", name);
+}
+
+int lg_get_field(lg_domain *d, const char *name, void *dst, size_t n)
+{
+    if (!d || !name || (!dst && n)) return set_error(LG_ERR_INVALID, "null argument");
+    int st;
+    if (d->host_only) {
+        if (std::vector<double> *hv = find_f64_host(d, name)) {
+            if (n != hv->size())
+                return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name,
+                                 hv->size(), n);
+            memcpy(dst, hv->data(), n * sizeof(double));
+            return LG_OK;
+        }
+    } else if ((st = ensure_device(d))) {
+        return st;
+    }
+    double *p;
+    size_t c;
+    if (!d->host_only && find_f64(d, name, &p, &c)) {
+        if (n != c) return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, c, n);
+        LG_CUDA(cudaMemcpyAsync(dst, p, c * sizeof(double), cudaMemcpyDeviceToHost, d->stream));
+        LG_CUDA(cudaStreamSynchronize(d->stream));
+        return LG_OK;
+    }
+    if (std::vector<int> *v = find_i32(d, name)) {
+        if (n != v->size())
+            return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, v->size(), n);
+        if (n) memcpy(dst, v->data(), n * sizeof(int));
+        return LG_OK;
+    }
+    return set_error(LG_ERR_INVALID, "unknown field '%s'", name);
+}
+
+int lg_set_field(lg_domain *d, const char *name, const void *src, size_t n)
+{
+    if (!d || !name || (!src && n)) return set_error(LG_ERR_INVALID, "null argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    double *p;
+    size_t c;
+    if (find_f64(d, name, &p, &c)) {
+        if (n != c) return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, c, n);
+        LG_CUDA(cudaMemcpyAsync(p, src, c * sizeof(double), cudaMemcpyHostToDevice, d->stream));
+        LG_CUDA(cudaStreamSynchronize(d->stream));
+        return LG_OK;
+    }
+    std::vector<int> *v = find_i32(d, name);
+    if (!v) return set_error(LG_ERR_INVALID, "unknown field '%s'", name);
+    if (n != v->size())
+        return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, v->size(), n);
+    lg::Problem &pr = d->prob;
+    const int *in = static_cast<const int *>(src);
+    if (!strcmp(name, "regElemSize") || !strcmp(name, "nodeElemStart") ||
+        !strcmp(name, "nodeElemCornerList") || !strcmp(name, "symmX") ||
+        !strcmp(name, "symmY") || !strcmp(name, "symmZ"))
+        return set_error(LG_ERR_INVALID, "field '%s' is derived and read-only", name);
+    if (!strcmp(name, "nodelist")) {
+        for (size_t i = 0; i < n; ++i)
+            if (in[i] < 0 || in[i] >= pr.numNode)
+                return set_error(LG_ERR_INVALID, "nodelist entry %zu out of range", i);
+    } else if (!strcmp(name, "regNumList")) {
+        for (size_t i = 0; i < n; ++i)
+            if (in[i] < 1 || in[i] > pr.numReg)
+                return set_error(LG_ERR_INVALID, "regNumList entry %zu out of range", i);
+    } else if (strcmp(name, "elemBC") != 0) {
+        for (size_t i = 0; i < n; ++i)
+            if (in[i] < 0 || in[i] >= pr.numElem)
+                return set_error(LG_ERR_INVALID, "%s entry %zu out of range", name, i);
+    }
+    std::copy(in, in + n, v->begin());
+    if (!strcmp(name, "nodelist")) lg::build_corner_list(pr);
+    if (!strcmp(name, "regNumList")) lg::build_region_sets(pr);
+    return upload_topology(d);
+}
+
+int lg_get_scalar(lg_domain *d, const char *name, double *value)
+{
+    if (!d || !name || !value) return set_error(LG_ERR_INVALID, "null argument");
+    int st;
+    lg::Ctl hc{};
+    if (d->host_only) {
+        const lg::TimeState &t = d->prob.t;
+        hc.time = t.time; hc.deltatime = t.deltatime; hc.dtcourant = t.dtcourant;
+        hc.dthydro = t.dthydro; hc.stoptime = t.stoptime; hc.dtmax = t.dtmax;
+        hc.dtfixed = t.dtfixed; hc.dtmultlb = t.deltatimemultlb;
+        hc.dtmultub = t.deltatimemultub; hc.cycle = t.cycle;
+    } else {
+        if ((st = ensure_device(d))) return st;
+        if ((st = read_ctl(d))) return st;
+        hc = *d->h_ctl;
+    }
+    const lg::Ctl &c = hc;
+    const lg::Problem &p = d->prob;
+    struct { const char *n; double v; } t[] = {
+        {"time", c.time}, {"deltatime", c.deltatime}, {"dtcourant", c.dtcourant},
+        {"dthydro", c.dthydro}, {"stoptime", c.stoptime}, {"dtmax", c.dtmax},
+        {"dtfixed", c.dtfixed}, {"deltatimemultlb", c.dtmultlb},
+        {"deltatimemultub", c.dtmultub}, {"hgcoef", d->ds.prm.hgcoef},
+        {"cycle", (double)c.cycle}, {"its", (double)d->its}, {"numElem", (double)p.numElem},
+        {"numNode", (double)p.numNode}, {"numReg", (double)p.numReg},
+        {"sizeX", (double)p.nx}, {"cost", (double)p.cost}, {"status", (double)c.status},
+        {"launches", (double)d->launches}};
+    for (auto &f : t)
+        if (!strcmp(f.n, name)) {
+            *value = f.v;
+            return LG_OK;
+        }
+    return set_error(LG_ERR_INVALID, "unknown scalar '%s'", name);
+}
+
+int lg_set_scalar(lg_domain *d, const char *name, double value)
+{
+    if (!d || !name) return set_error(LG_ERR_INVALID, "null argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    if (!strcmp(name, "hgcoef")) {
+        d->ds.prm.hgcoef = value;
+        drop_graphs(d);  // the kernel arguments are baked into the graphs
+        return LG_OK;
+    }
+    if (!strcmp(name, "its")) {
+        d->its = (int)value;
+        return LG_OK;
+    }
+    if ((st = read_ctl(d))) return st;
+    lg::Ctl &c = *d->h_ctl;
+    struct { const char *n; double *v; } t[] = {
+        {"time", &c.time}, {"deltatime", &c.deltatime}, {"dtcourant", &c.dtcourant},
+        {"dthydro", &c.dthydro}, {"stoptime", &c.stoptime}, {"dtmax", &c.dtmax},
+        {"dtfixed", &c.dtfixed}, {"deltatimemultlb", &c.dtmultlb},
+        {"deltatimemultub", &c.dtmultub}};
+    for (auto &f : t)
+        if (!strcmp(f.n, name)) {
+            *f.v = value;
+            return write_ctl(d);
+        }
+    if (!strcmp(name, "cycle")) {
+        c.cycle = (int)value;
+        return write_ctl(d);
+    }
+    if (!strcmp(name, "status")) {  // clear a recorded error
+        c.status = (int)value;
+        return write_ctl(d);
+    }
+    return set_error(LG_ERR_INVALID, "unknown or read-only scalar '%s'", name);
+}
+
+int lg_region_rep(lg_domain *d, int r, int *rep)
+{
+    if (!d || !rep || r < 0 || r >= d->prob.numReg) return set_error(LG_ERR_INVALID, "invalid region");
+    *rep = lg::region_rep(r, d->prob.numReg, d->prob.cost);
+    return LG_OK;
+}
+
+int lg_verify(lg_domain *d, double out[4])
+{
+    if (!d || !out) return set_error(LG_ERR_INVALID, "null argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    const int nx = d->prob.nx;
+    std::vector<double> e((size_t)nx * nx);
+    LG_CUDA(cudaMemcpyAsync(e.data(), d->ds.e, e.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                            d->stream));
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    // lulesh-util.cc:197-212, same summation order
+    double MaxAbsDiff = 0.0, TotalAbsDiff = 0.0, MaxRelDiff = 0.0;
+    for (int j = 0; j < nx; ++j)
+        for (int k = j + 1; k < nx; ++k) {
+            const double AbsDiff = std::fabs(e[(size_t)j * nx + k] - e[(size_t)k * nx + j]);
+            TotalAbsDiff += AbsDiff;
+            if (MaxAbsDiff < AbsDiff) MaxAbsDiff = AbsDiff;
+            const double RelDiff = AbsDiff / e[(size_t)k * nx + j];
+            if (MaxRelDiff < RelDiff) MaxRelDiff = RelDiff;
+        }
+    out[0] = e[0];
+    out[1] = MaxAbsDiff;
+    out[2] = TotalAbsDiff;
+    out[3] = MaxRelDiff;
+    return LG_OK;
+}
+
+int lg_report(lg_domain *d, double elapsed, char *buf, size_t buflen)
+{
+    if (!d || !buf || !buflen) return set_error(LG_ERR_INVALID, "null argument");
+    double v[4];
+    int st;
+    if ((st = lg_verify(d, v))) return st;
+    if ((st = read_ctl(d))) return st;
+    const std::string s = lg::format_report(d->prob.nx, d->h_ctl->cycle, v[0], v[1], v[2], v[3],
+                                            elapsed);
+    snprintf(buf, buflen, "%s", s.c_str());
+    return LG_OK;
+}
+
+int lg_profile(lg_domain *d, int ncycles, double *ms, const char **names, int *nkernels)
+{
+    if (!d || !ms || !nkernels || *nkernels < lg::K_COUNT)
+        return set_error(LG_ERR_INVALID, "invalid argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    if ((st = read_ctl(d))) return st;
+    if (d->h_ctl->status != 0) return d->h_ctl->status;
+    const int lim = (int)std::min<long long>(d->its, (long long)d->h_ctl->cycle + ncycles);
+    LG_CUDA(cudaMemcpyAsync(&d->ds.ctl->cycle_limit, &lim, sizeof(int), cudaMemcpyHostToDevice,
+                            d->stream));
+    std::vector<cudaEvent_t> ev(2 * lg::K_COUNT * (size_t)ncycles);
+    for (auto &e : ev) LG_CUDA(cudaEventCreate(&e));
+    d->ks->begin(d->ds.ctl, d->stream);
+    for (int c = 0; c < ncycles; ++c)
+        for (int k = 0; k < lg::K_COUNT; ++k) {
+            LG_CUDA(cudaEventRecord(ev[2 * (c * lg::K_COUNT + k)], d->stream));
+            d->ks->launch(k, d->ds, k == lg::K_MATERIAL ? 2 : 0, d->stream);
+            LG_CUDA(cudaEventRecord(ev[2 * (c * lg::K_COUNT + k) + 1], d->stream));
+        }
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    for (int k = 0; k < lg::K_COUNT; ++k) {
+        ms[k] = 0.0;
+        if (names) names[k] = d->ks->kernel_names[k];
+    }
+    for (int c = 0; c < ncycles; ++c)
+        for (int k = 0; k < lg::K_COUNT; ++k) {
+            float f = 0.f;
+            LG_CUDA(cudaEventElapsedTime(&f, ev[2 * (c * lg::K_COUNT + k)],
+                                         ev[2 * (c * lg::K_COUNT + k) + 1]));
+            ms[k] += f;
+        }
+    for (auto &e : ev) cudaEventDestroy(e);
+    *nkernels = lg::K_COUNT;
+    if ((st = read_ctl(d))) return st;
+    return d->h_ctl->status;
+}
+
+}  // extern "C"
