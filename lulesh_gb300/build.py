@@ -88,13 +88,16 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         o = os.path.join(OBJ, src + ".o")
         objs.append(o)
         if _stale(o, [s] + hdrs):
-            steps.append(["g++", "-O2", "-std=c++17", "-fPIC", "-I" + CSRC,
+            # no FMA contraction: set-up arithmetic (volumes, masses, the first
+            # time step) must round exactly as the reference's on every host
+            # (GCC contracts by default on aarch64)
+            steps.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + CSRC,
                           "-I" + os.path.join(ROOT, "include"), "-c", s, "-o", o])
     cli_src = os.path.join(CSRC, "lulesh_gpu.cc")
     cli_obj = os.path.join(OBJ, "lulesh_gpu.cc.o")
     if _stale(cli_obj, [cli_src] + hdrs):
-        steps.append(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
-                      "-c", cli_src, "-o", cli_obj])
+        steps.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                      "-I" + os.path.join(ROOT, "include"), "-c", cli_src, "-o", cli_obj])
     with ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         for cmd in steps:
             if verbose:

@@ -1,0 +1,96 @@
+"""The benchmark mesh (s=150, 3,375,000 elements) through size-independent
+properties, plus an opt-in field-by-field comparison with the oracle after the
+full 500 cycles (set LG_FULL=1; the CPU oracle takes minutes).
+
+Properties of the Sedov problem that hold at any size:
+  * the solution is symmetric under every permutation of the x, y, z axes
+    (the blast sits in the corner element, the mesh and the boundary
+    conditions are symmetric); the reference checks the x<->y case on plane 0
+    (lulesh-util.cc:197-218) and finds rounding-level deltas;
+  * element and nodal masses and reference volumes never change;
+  * two runs are bitwise identical.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from paritylib import FP64_TOL, compare_states
+
+pytestmark = pytest.mark.gpu
+
+# symmetry deltas are rounding-level: normwise ~1e-16 for e and v and ~3e-15
+# for p after 100 cycles at s=30 and s=150, on the GPU and in the oracle
+SYMM_TOL = 1e-12
+
+
+def _perms(a3):
+    yield "xy", np.transpose(a3, (0, 2, 1))
+    yield "xz", np.transpose(a3, (2, 1, 0))
+    yield "yz", np.transpose(a3, (1, 0, 2))
+
+
+@pytest.fixture(scope="module")
+def big(native_lib):
+    import lulesh_gb300 as lg
+    d = lg.Domain(150, its=100)
+    assert d.run() == 0
+    yield d
+    d.close()
+
+
+def test_s150_axis_permutation_symmetry(big):
+    n = 150
+    for f in ("e", "p", "q", "v", "ss"):
+        a3 = big.field(f).reshape(n, n, n)
+        scale = np.max(np.abs(a3))
+        for name, t in _perms(a3):
+            err = np.max(np.abs(a3 - t)) / scale
+            assert err <= SYMM_TOL, (f, name, err)
+    # nodal: x(i,j,k) == y(j,i,k) and the velocities alike
+    m = n + 1
+    x = big.field("x").reshape(m, m, m)
+    y = big.field("y").reshape(m, m, m)
+    assert np.max(np.abs(x - np.transpose(y, (0, 2, 1)))) <= SYMM_TOL * np.max(np.abs(x))
+    xd = big.field("xd").reshape(m, m, m)
+    yd = big.field("yd").reshape(m, m, m)
+    assert np.max(np.abs(xd - np.transpose(yd, (0, 2, 1)))) <= SYMM_TOL * np.max(np.abs(xd))
+
+
+def test_s150_masses_and_reference_volumes_unchanged(big, native_lib):
+    import lulesh_gb300 as lg
+    d0 = lg.Domain(150, device=-1)  # the set-up values, built on the host
+    for f in ("nodalMass", "elemMass", "volo"):
+        assert np.array_equal(big.field(f).view(np.int64), d0.field(f).view(np.int64)), f
+
+
+def test_s150_deterministic(big, native_lib):
+    import lulesh_gb300 as lg
+    d = lg.Domain(150, its=100)
+    assert d.run() == 0
+    for f in ("x", "xd", "e", "p", "q", "v", "ss"):
+        assert np.array_equal(d.field(f).view(np.int64), big.field(f).view(np.int64)), f
+    d.close()
+
+
+@pytest.mark.skipif(os.environ.get("LG_FULL") != "1", reason="set LG_FULL=1 (minutes of CPU)")
+@pytest.mark.parametrize("precision", ["fp64", "fp64-fma"])
+def test_s150_500_cycles_vs_oracle(native_lib, oracle_built, precision, capsys):
+    import lulesh_gb300 as lg
+    from oracle.oracle import OracleDomain
+    global _ORACLE_500
+    try:
+        ref = _ORACLE_500
+    except NameError:
+        o = OracleDomain(150)
+        assert o.step(500) == 0
+        ref = _ORACLE_500 = o.state()
+        o.close()
+    d = lg.Domain(150, its=500, precision=precision)
+    assert d.run() == 0
+    errs = compare_states(d.state(), ref, lg.NODE_FIELDS + lg.ELEM_FIELDS)
+    with capsys.disabled():
+        print(f"\n{precision} s=150 500 cycles: worst "
+              f"{max(errs, key=errs.get)}={max(errs.values()):.3e}",
+              {k: f"{v:.1e}" for k, v in errs.items()})
+    assert max(errs.values()) <= FP64_TOL, errs
