@@ -141,6 +141,40 @@ int lg_reset(lg_domain *d);
  * The FP64 leap-frog path is bound by this rate, not by HBM bandwidth. */
 int lg_measure_pipe(int op, int fp32, double *ginst_per_s);
 
+/* Nodal forces with no device allocation, for callers that own all device
+ * memory themselves.  No counterpart in the reference: it exists for codes
+ * that cannot let a library allocate behind their back -- hydro codes that
+ * carve every device buffer from one pool sized at start-up, processes under
+ * a hard per-GPU memory budget, and time-step loops that must not pay for the
+ * device-wide synchronisation of cudaFree or an allocation failing mid-run.
+ *
+ * Computes fx, fy, fz of CalcForceForNodes (stress integration, FB hourglass
+ * forces and the ordered per-node corner gather; lulesh.cc:1104-1135) from
+ * the caller's device arrays: nodelist (8*numElem, element-major as
+ * Domain::nodelist), nodeElemStart (numNode+1) and nodeElemCornerList
+ * (8*numElem) as built by lulesh-init.cc:272-337, node fields x..zd
+ * (numNode), element fields p q v volo ss elemMass (numElem), hgcoef; writes
+ * fx, fy, fz (numNode).  stream is a cudaStream_t or NULL; the call waits for
+ * its work to finish and returns 0, -1 (VolumeError: a non-positive volume)
+ * or an LG_ERR_* code.
+ *
+ * It calls no cudaMalloc, cudaFree or allocating routine.  Its per-corner
+ * scratch is one fixed static device array of 48 doubles per element for at
+ * most 32768 elements (about 12.6 MB, held on every GPU where the call has
+ * run until the process exits); larger meshes are rejected with
+ * LG_ERR_INVALID.  The first call on each device looks up that array's
+ * device address, so make it before any stream capture on that device.  All
+ * calls share the array: calls whose work overlaps on one GPU race and must
+ * be serialised by the caller. */
+int lg_calc_force_for_nodes_noalloc(int numElem, int numNode, const int *nodelist,
+                                    const int *nodeElemStart, const int *nodeElemCornerList,
+                                    const double *x, const double *y, const double *z,
+                                    const double *xd, const double *yd, const double *zd,
+                                    const double *p, const double *q, const double *v,
+                                    const double *volo, const double *ss,
+                                    const double *elemMass, double hgcoef, double *fx,
+                                    double *fy, double *fz, void *stream);
+
 /* Human-readable description of the most recent error on this thread. */
 const char *lg_last_error(void);
 

@@ -36,6 +36,7 @@ CUDA_UNITS = [
     ("lg_kernels_mixed.cu", ["--fmad=true"]),
     ("lg_api.cu", []),
     ("lg_peak.cu", ["--fmad=true"]),
+    ("lg_noalloc.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["lg_problem.cc"]
 

@@ -55,6 +55,10 @@ struct Layout {
 
 }  // namespace
 
+namespace lg {
+int record_error(int code, const char *msg) { return set_error(code, "%s", msg); }
+}  // namespace lg
+
 struct lg_domain {
     lg_opts opts{};
     lg::Problem prob;  // host mirror: integer fields and the initial state
