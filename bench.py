@@ -197,6 +197,38 @@ def cpu_reference_rate(a, budget_s: float, warmup: int, max_cycles: int) -> dict
                       f"untimed); oracle C restatement -O3 -fopenmp, {threads} threads"}
 
 
+def _total_energy(d) -> float:
+    import numpy as np
+    m = d.field("nodalMass")
+    ke = 0.5 * np.sum(m * (d.field("xd") ** 2 + d.field("yd") ** 2 + d.field("zd") ** 2))
+    return float(np.sum(d.field("e") * d.field("volo")) + ke)
+
+
+def error_vs_fp64(a, d) -> dict:
+    """Errors of handle d (after K cycles) against an FP64 run of the same cycles."""
+    import numpy as np
+    import lulesh_gb300 as lg
+    d.reset()
+    d.step(a.steps)
+    ref = lg.Domain(a.nx, a.regions, a.balance, a.cost, its=10 ** 9, precision="fp64",
+                    device=d_device(d))
+    ref.step(a.steps)
+    vm, vf = d.verify(), ref.verify()
+    em, ef = d.field("e"), ref.field("e")
+    out = {"cycles": a.steps,
+           "origin_energy_rel": abs(vm["origin_energy"] / vf["origin_energy"] - 1),
+           "total_energy_rel": abs(_total_energy(d) / _total_energy(ref) - 1),
+           "e_normwise": float(np.max(np.abs(em - ef)) / np.max(np.abs(ef))),
+           "symmetry_MaxRelDiff": vm["MaxRelDiff"], "symmetry_MaxRelDiff_fp64": vf["MaxRelDiff"],
+           "symmetry_MaxAbsDiff": vm["MaxAbsDiff"], "symmetry_MaxAbsDiff_fp64": vf["MaxAbsDiff"]}
+    ref.close()
+    return out
+
+
+def d_device(d) -> int:
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
 def run_reference(a):
     dist, ws, rank, local = _dist()
     if rank != 0:
@@ -304,6 +336,8 @@ def run_gpu(a):
             "config": _workload(a), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "roofline_fp64": roof64, "clocks": clk.summary(),
             "origin_energy": verify["origin_energy"]}
+    if a.err_vs_fp64 and a.precision != "fp64":
+        line["err_vs_fp64"] = error_vs_fp64(a, d)
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference_rate(
             a, budget_s=float(os.environ.get("LG_CPU_BUDGET_S", "15")), warmup=1,
@@ -324,6 +358,9 @@ def main():
     p.add_argument("--cost", type=int, default=1)
     p.add_argument("--precision", default="fp64", choices=["fp64", "fp64-fma", "mixed"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--err-vs-fp64", action="store_true",
+                   help="after timing, rerun the workload in FP64 (untimed) and report the "
+                        "origin-energy, total-energy and field errors of this precision")
     a = p.parse_args()
     if a.warmup < 0 or a.steps < 1:
         p.error("need --steps >= 1 and --warmup >= 0")

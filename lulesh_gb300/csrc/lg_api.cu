@@ -113,6 +113,14 @@ int upload(lg_domain *d, T *dst, const std::vector<T> &src)
     return LG_OK;
 }
 
+// 1 / nodalMass for the mixed path's acceleration, from the host values m
+int upload_inv_mass(lg_domain *d, const double *m, size_t n)
+{
+    std::vector<double> inv(n);
+    for (size_t i = 0; i < n; ++i) inv[i] = 1.0 / m[i];
+    return upload(d, d->ds.invMass, inv);
+}
+
 // Kernel-side layouts derived from the integer fields (see lg_device.h).
 int upload_topology(lg_domain *d)
 {
@@ -300,6 +308,7 @@ int upload_initial_state(lg_domain *d)
         if ((st = upload(d, fld, *hostf[i]))) return st;
     }
     if ((st = upload_topology(d))) return st;
+    if ((st = upload_inv_mass(d, p.nodalMass.data(), p.nodalMass.size()))) return st;
 
     lg::Ctl &c = *d->h_ctl;
     memset(&c, 0, sizeof(c));
@@ -350,6 +359,7 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     switch (opts->precision) {
     case LG_FP64: ks = lg::kernels_fp64_strict(); break;
     case LG_FP64_FMA: ks = lg::kernels_fp64_fma(); break;
+    case LG_MIXED: ks = lg::kernels_mixed(); break;
     default: return set_error(LG_ERR_INVALID, "precision %d not available", opts->precision);
     }
     lg_domain *d = new lg_domain();
@@ -376,7 +386,7 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     const int eblocks = (int)((E + 127) / 128);
 
     Layout L;
-    size_t o_node[13], o_elem[19];
+    size_t o_node[14], o_elem[19];
     for (auto &o : o_node) o = L.add<double>(N);
     for (auto &o : o_elem) o = L.add<double>(E);
     const size_t o_corner = L.add<double>(48 * E);
@@ -401,9 +411,9 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     s.N = (int)N;
     s.nx = p.nx;
     s.numReg = p.numReg;
-    double **nodef[13] = {&s.x, &s.y, &s.z, &s.xd, &s.yd, &s.zd, &s.xdd, &s.ydd, &s.zdd,
-                          &s.fx, &s.fy, &s.fz, &s.nodalMass};
-    for (int i = 0; i < 13; ++i) *nodef[i] = reinterpret_cast<double *>(base + o_node[i]);
+    double **nodef[14] = {&s.x, &s.y, &s.z, &s.xd, &s.yd, &s.zd, &s.xdd, &s.ydd, &s.zdd,
+                          &s.fx, &s.fy, &s.fz, &s.nodalMass, &s.invMass};
+    for (int i = 0; i < 14; ++i) *nodef[i] = reinterpret_cast<double *>(base + o_node[i]);
     double **elemf[19] = {&s.e, &s.p, &s.q, &s.ql, &s.qq, &s.v, &s.volo, &s.vnew, &s.delv,
                           &s.vdov, &s.arealg, &s.ss, &s.elemMass, &s.delx_xi, &s.delx_eta,
                           &s.delx_zeta, &s.delv_xi, &s.delv_eta, &s.delv_zeta};
@@ -590,6 +600,8 @@ int lg_get_field(lg_domain *d, const char *name, void *dst, size_t n)
     }
     double *p;
     size_t c;
+    if (d->opts.precision == LG_MIXED && !strncmp(name, "del", 3) && strcmp(name, "delv") != 0)
+        return set_error(LG_ERR_INVALID, "'%s' is held in FP32 by the mixed path", name);
     if (!d->host_only && find_f64(d, name, &p, &c)) {
         if (n != c) return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, c, n);
         LG_CUDA(cudaMemcpyAsync(dst, p, c * sizeof(double), cudaMemcpyDeviceToHost, d->stream));
@@ -615,6 +627,9 @@ int lg_set_field(lg_domain *d, const char *name, const void *src, size_t n)
     if (find_f64(d, name, &p, &c)) {
         if (n != c) return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, c, n);
         LG_CUDA(cudaMemcpyAsync(p, src, c * sizeof(double), cudaMemcpyHostToDevice, d->stream));
+        if (!strcmp(name, "nodalMass") &&
+            (st = upload_inv_mass(d, static_cast<const double *>(src), c)))
+            return st;
         LG_CUDA(cudaStreamSynchronize(d->stream));
         return LG_OK;
     }

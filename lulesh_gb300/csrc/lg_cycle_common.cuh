@@ -1,0 +1,305 @@
+// lg_cycle_common.cuh -- the cycle's control logic and the per-element EOS,
+// shared by the FP64 and mixed kernel sets.  Included once per kernel
+// translation unit inside namespace lg::LG_NS (each unit is compiled with its
+// own FMA setting).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lg_device.h"
+
+#ifndef LG_NS
+#error "define LG_NS"
+#endif
+
+namespace lg {
+namespace LG_NS {
+
+constexpr int kBlock = 128;
+
+// Keeps the compiler from treating a value as loop-invariant, so that every
+// EOS repetition the reference performs is evaluated.
+__device__ __forceinline__ void opaque(double &v) { asm volatile("" : "+d"(v)); }
+
+__device__ __forceinline__ void raise_status(Ctl *c, int code) { atomicCAS(&c->status, 0, code); }
+
+// TimeIncrement, lulesh.cc:166-222
+__device__ __forceinline__ void time_increment(Ctl *c)
+{
+    double targetdt = c->stoptime - c->time;
+    if ((c->dtfixed <= 0.0) && (c->cycle != 0)) {
+        double ratio;
+        const double olddt = c->deltatime;
+        double gnewdt = 1.0e+20;
+        double newdt;
+        if (c->dtcourant < gnewdt) gnewdt = c->dtcourant / 2.0;
+        if (c->dthydro < gnewdt) gnewdt = c->dthydro * 2.0 / 3.0;
+        newdt = gnewdt;
+        ratio = newdt / olddt;
+        if (ratio >= 1.0) {
+            if (ratio < c->dtmultlb)
+                newdt = olddt;
+            else if (ratio > c->dtmultub)
+                newdt = olddt * c->dtmultub;
+        }
+        if (newdt > c->dtmax) newdt = c->dtmax;
+        c->deltatime = newdt;
+    }
+    if ((targetdt > c->deltatime) && (targetdt < (4.0 * c->deltatime / 3.0)))
+        targetdt = 2.0 * c->deltatime / 3.0;
+    if (targetdt < c->deltatime) c->deltatime = targetdt;
+    c->time += c->deltatime;
+    ++c->cycle;
+}
+
+// Loop condition of lulesh.cc:2745 followed by TimeIncrement.
+__device__ __forceinline__ void begin_cycle(Ctl *c)
+{
+    if (c->status == 0 && c->time < c->stoptime && c->cycle < c->cycle_limit) {
+        time_increment(c);
+        c->active = 1;
+    } else {
+        c->active = 0;
+    }
+}
+
+__global__ void k_begin(Ctl *c) { begin_cycle(c); }
+__global__ void k_time_increment(Ctl *c)
+{
+    time_increment(c);
+    c->active = 1;
+}
+__global__ void k_set_active(Ctl *c) { c->active = 1; }
+
+__device__ __forceinline__ bool cycle_live(const Ctl *c) { return c->active && c->status == 0; }
+
+
+// ---------------------------------------------------------------------------
+// k_material
+// ---------------------------------------------------------------------------
+
+// one direction of CalcMonotonicQRegionForElems, lulesh.cc:1778-1813
+template <typename R>
+__device__ __forceinline__ R monoq_phi(R limiter_mult, R max_slope, const R *dv, int ielem, int bc,
+                                       int msymm, int mfree, int mmask, int psymm, int pfree,
+                                       int pmask, int nbm, int nbp)
+{
+    const R ptiny = R(1.e-36);
+    R delvm, delvp;
+    const R self = dv[ielem];
+    const R norm = R(1.) / (self + ptiny);
+    const int bm = bc & mmask, bp = bc & pmask;
+    if (bm == msymm)
+        delvm = self;
+    else if (bm == mfree)
+        delvm = R(0.0);
+    else if (bm == 0 || bm == (mmask & ~(msymm | mfree)))
+        delvm = dv[nbm];
+    else
+        delvm = R(0);
+    if (bp == psymm)
+        delvp = self;
+    else if (bp == pfree)
+        delvp = R(0.0);
+    else if (bp == 0 || bp == (pmask & ~(psymm | pfree)))
+        delvp = dv[nbp];
+    else
+        delvp = R(0);
+    delvm = delvm * norm;
+    delvp = delvp * norm;
+    R phi = R(.5) * (delvm + delvp);
+    delvm *= limiter_mult;
+    delvp *= limiter_mult;
+    if (delvm < phi) phi = delvm;
+    if (delvp < phi) phi = delvp;
+    if (phi < R(0.)) phi = R(0.);
+    if (phi > max_slope) phi = max_slope;
+    return phi;
+}
+
+// The reference's FP64 arithmetic for the EOS: IEEE division and square root
+// and ordinary comparisons.  lg_fastmath.cuh has the mixed path's variant
+// with the same interface.
+struct IeeeOps {
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    static __device__ __forceinline__ double sqrt_(double a) { return sqrt(a); }
+    static __device__ __forceinline__ bool lt(double a, double b) { return a < b; }
+    static __device__ __forceinline__ bool le(double a, double b) { return a <= b; }
+    // |a| < b
+    static __device__ __forceinline__ bool abs_lt(double a, double b) { return fabs(a) < b; }
+};
+
+// sound-speed term of lulesh.cc:2083-2090, 2126-2133, 2158-2165, 2190-2197
+template <class M = IeeeOps>
+__device__ __forceinline__ double ssc_of(double num, double rho0)
+{
+    double ssc = (rho0 == 1.0) ? num : M::div(num, rho0);
+    if (M::le(ssc, .1111111e-36))
+        ssc = .3333333e-18;
+    else
+        ssc = M::sqrt_(ssc);
+    return ssc;
+}
+
+// CalcPressureForElems for one element, lulesh.cc:2014-2044
+template <class M = IeeeOps>
+__device__ __forceinline__ double pressure(const Params &P, double &bvc, double &pbvc,
+                                           double e_old, double compression, double vnewc)
+{
+    const double c1s = 2.0 / 3.0;
+    bvc = c1s * (compression + 1.);
+    pbvc = c1s;
+    double p_new = bvc * e_old;
+    if (M::abs_lt(p_new, P.p_cut)) p_new = 0.0;
+    if (M::le(P.eosvmax, vnewc)) p_new = 0.0;  // vnewc >= eosvmax
+    if (M::lt(p_new, P.pmin)) p_new = P.pmin;
+    return p_new;
+}
+
+// EvalEOSForElems for one element (lulesh.cc:2204-2324) with
+// CalcEnergyForElems (2048-2176) and CalcSoundSpeedForElems (2180-2200).
+// All rep repetitions are evaluated, as in the reference.
+template <class M = IeeeOps>
+__device__ __forceinline__ void eval_eos(const Params &P, double e_in, double delv_in,
+                                         double p_in, double q_in, double qq_in, double ql_in,
+                                         double vnewc, int rep, double &p_out, double &e_out,
+                                         double &q_out, double &ss_out)
+{
+    const double rho0 = P.refdens;
+    double p_new = 0., e_new = 0., q_new = 0., bvc = 0., pbvc = 0.;
+    for (int j = 0; j < rep; j++) {
+        double e_old = e_in, delvc = delv_in, p_old = p_in, q_old = q_in, qq_old = qq_in,
+               ql_old = ql_in, vc = vnewc;
+        opaque(e_old); opaque(delvc); opaque(p_old); opaque(q_old);
+        opaque(qq_old); opaque(ql_old); opaque(vc);
+        double compression = M::div(1., vc) - 1.;
+        const double vchalf = vc - delvc * .5;
+        double compHalfStep = M::div(1., vchalf) - 1.;
+        if (P.eosvmin != 0. && M::le(vc, P.eosvmin)) compHalfStep = compression;
+        if (P.eosvmax != 0. && M::le(P.eosvmax, vc)) {
+            p_old = 0.;
+            compression = 0.;
+            compHalfStep = 0.;
+        }
+        const double work = 0.;
+
+        e_new = e_old - .5 * delvc * (p_old + q_old) + .5 * work;
+        if (M::lt(e_new, P.emin)) e_new = P.emin;
+
+        const double pHalfStep = pressure<M>(P, bvc, pbvc, e_new, compHalfStep, vc);
+        const double vhalf = M::div(1., 1. + compHalfStep);
+        if (M::lt(0., delvc)) {
+            q_new = 0.;
+        } else {
+            const double ssc = ssc_of<M>(pbvc * e_new + vhalf * vhalf * bvc * pHalfStep, rho0);
+            q_new = (ssc * ql_old + qq_old);
+        }
+        e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (pHalfStep + q_new));
+
+        e_new += .5 * work;
+        if (M::abs_lt(e_new, P.e_cut)) e_new = 0.;
+        if (M::lt(e_new, P.emin)) e_new = P.emin;
+
+        p_new = pressure<M>(P, bvc, pbvc, e_new, compression, vc);
+        {
+            const double sixth = 1.0 / 6.0;
+            double q_tilde;
+            if (M::lt(0., delvc)) {
+                q_tilde = 0.;
+            } else {
+                const double ssc = ssc_of<M>(pbvc * e_new + vc * vc * bvc * p_new, rho0);
+                q_tilde = (ssc * ql_old + qq_old);
+            }
+            e_new = e_new - (7.0 * (p_old + q_old) - 8.0 * (pHalfStep + q_new) +
+                             (p_new + q_tilde)) * delvc * sixth;
+            if (M::abs_lt(e_new, P.e_cut)) e_new = 0.;
+            if (M::lt(e_new, P.emin)) e_new = P.emin;
+        }
+
+        p_new = pressure<M>(P, bvc, pbvc, e_new, compression, vc);
+        if (M::le(delvc, 0.)) {
+            const double ssc = ssc_of<M>(pbvc * e_new + vc * vc * bvc * p_new, rho0);
+            q_new = (ssc * ql_old + qq_old);
+            if (M::abs_lt(q_new, P.q_cut)) q_new = 0.;
+        }
+    }
+    p_out = p_new;
+    e_out = e_new;
+    q_out = q_new;
+    ss_out = ssc_of<M>(pbvc * e_new + vnewc * vnewc * bvc * p_new, rho0);
+}
+
+__device__ __forceinline__ double dmin_sel(double a, double b) { return (b < a) ? b : a; }
+
+// Reduces (dtc, dth) over the block; the last block of the grid reduces the
+// per-block results into ctl->dtcourant/dthydro, merges error flags and, if
+// advance, evaluates the loop condition and TimeIncrement of the next cycle.
+__device__ __forceinline__ void finish_dt(DevState &s, double dtc, double dth, bool advance)
+{
+    __shared__ double red[2][kBlock / 32];
+    __shared__ bool am_last;
+    Ctl *ctl = s.ctl;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        dtc = dmin_sel(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
+        dth = dmin_sel(dth, __shfl_down_sync(0xffffffffu, dth, off));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][warp] = dtc;
+        red[1][warp] = dth;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bc = red[0][0], bh = red[1][0];
+        for (int w = 1; w < kBlock / 32; ++w) {
+            bc = dmin_sel(bc, red[0][w]);
+            bh = dmin_sel(bh, red[1][w]);
+        }
+        s.dt_partial[2 * blockIdx.x] = bc;
+        s.dt_partial[2 * blockIdx.x + 1] = bh;
+        __threadfence();
+        const unsigned prev = atomicAdd(&ctl->blocks_done, 1u);
+        am_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!am_last) return;
+    __threadfence();
+    double c = 1.0e+20, h = 1.0e+20;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+        c = dmin_sel(c, __ldcg(&s.dt_partial[2 * i]));
+        h = dmin_sel(h, __ldcg(&s.dt_partial[2 * i + 1]));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        c = dmin_sel(c, __shfl_down_sync(0xffffffffu, c, off));
+        h = dmin_sel(h, __shfl_down_sync(0xffffffffu, h, off));
+    }
+    __syncthreads();
+    if (lane == 0) {
+        red[0][warp] = c;
+        red[1][warp] = h;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kBlock / 32; ++w) {
+            red[0][0] = dmin_sel(red[0][0], red[0][w]);
+            red[1][0] = dmin_sel(red[1][0], red[1][w]);
+        }
+        ctl->dtcourant = red[0][0];
+        ctl->dthydro = red[1][0];
+        ctl->blocks_done = 0;
+        if (ctl->status == 0) {
+            if (ctl->err_qstop)
+                ctl->status = -2;
+            else if (ctl->err_matvol)
+                ctl->status = -1;
+        }
+        ctl->err_qstop = 0;
+        ctl->err_matvol = 0;
+        if (advance) begin_cycle(ctl);
+    }
+}
+
+}  // namespace LG_NS
+}  // namespace lg

@@ -6,7 +6,10 @@
 //                       eight corner loads of a warp are each coalesced;
 //   corner[c][j*E + e]  per-corner forces, c = 0..2 stress x/y/z and
 //                       c = 3..5 hourglass x/y/z, written coalesced by the
-//                       element kernel and gathered per node;
+//                       element kernel and gathered per node (FP32 values in
+//                       the same buffer for the mixed path, which also keeps
+//                       the monotonic-Q gradients as FP32 in the delx_* and
+//                       delv_* buffers);
 //   symm[n]             bit 0/1/2 set when node n is in symmX/Y/Z;
 //   regPerm[t], regRep[t]  region-sorted element order and the EOS
 //                       repetition count of position t (regions in order,
@@ -52,6 +55,7 @@ struct DevState {
     int E, N, nx, numReg;
     // node fields
     double *x, *y, *z, *xd, *yd, *zd, *xdd, *ydd, *zdd, *fx, *fy, *fz, *nodalMass;
+    double *invMass;  // 1 / nodalMass (mixed path)
     uint8_t *symm;
     int *nodeElemStart, *nodeElemCornerList;
     // element fields

@@ -1,0 +1,108 @@
+// lg_fastmath.cuh -- arithmetic helpers of the mixed-precision path.
+//
+// On GB300 the FP64 pipe issues at 1/74 of the FP32 rate, so the mixed path
+// keeps FP64 only where its accuracy is needed and moves everything exact or
+// approximate-enough elsewhere:
+//   * FP64 <-> FP32 conversions on the integer pipe (bit re-packing);
+//   * FP64 reciprocal and square root by Newton-Raphson refinement of the
+//     hardware approximations (PTX rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64):
+//     each step r <- r + r(1 - a r) squares the relative error, so two steps
+//     from the ~2^-20 seed leave the last bit or two of the double;
+//   * comparisons of doubles on the integer pipe through the order-preserving
+//     key of IEEE bit patterns (sign-magnitude -> two's complement order).
+// None of these is used by the FP64 paths.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace lg {
+namespace fast {
+
+// double -> float by re-biasing the exponent and truncating the mantissa
+// (round toward zero); values below the float normal range become zero,
+// values above it infinity.
+__device__ __forceinline__ float to_f32(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned r;
+    if (e <= 0)
+        r = sign;
+    else if (e >= 255)
+        r = sign | 0x7f800000u;
+    else
+        r = sign | ((unsigned)e << 23) | mant;
+    return __uint_as_float(r);
+}
+
+// float -> double, exact for normal values (float subnormals become zero).
+__device__ __forceinline__ double to_f64(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u;
+    const unsigned ex = (u >> 23) & 0xffu;
+    unsigned hi, lo;
+    if (ex == 0) {
+        hi = sign;
+        lo = 0;
+    } else {
+        const unsigned e64 = (ex == 255u) ? 0x7ffu : ex - 127u + 1023u;
+        hi = sign | (e64 << 20) | ((u & 0x7fffffu) >> 3);
+        lo = u << 29;
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ double rcp_nr(double a)
+{
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(a));
+    double e = fma(-a, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-a, r, 1.0);
+    return fma(r, e, r);
+}
+
+// sqrt(a) for a > 0: s = a * rsqrt(a), then two corrections
+// s <- s + (a - s^2) * (rsqrt(a) / 2)
+__device__ __forceinline__ double sqrt_nr(double a)
+{
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(a));
+    double s = a * y;
+    const double h = 0.5 * y;
+    double r = fma(-s, s, a);
+    s = fma(r, h, s);
+    r = fma(-s, s, a);
+    return fma(r, h, s);
+}
+
+// order-preserving integer key of a double (NaN excluded; -0 sorts just
+// below +0, the one difference from IEEE ordering)
+__device__ __forceinline__ unsigned long long order_key(double v)
+{
+    const long long b = __double_as_longlong(v);
+    const unsigned long long mask = (unsigned long long)(b >> 63) | 0x8000000000000000ull;
+    return (unsigned long long)b ^ mask;
+}
+
+// FP64 EOS operations of the mixed path (same interface as IeeeOps)
+struct FastOps {
+    static __device__ __forceinline__ double div(double a, double b) { return a * rcp_nr(b); }
+    static __device__ __forceinline__ double sqrt_(double a) { return sqrt_nr(a); }
+    static __device__ __forceinline__ bool lt(double a, double b) { return order_key(a) < order_key(b); }
+    static __device__ __forceinline__ bool le(double a, double b) { return order_key(a) <= order_key(b); }
+    // |a| < b for b >= 0: magnitude bits compare like the values
+    static __device__ __forceinline__ bool abs_lt(double a, double b)
+    {
+        return ((unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull) <
+               (unsigned long long)__double_as_longlong(b);
+    }
+};
+
+}  // namespace fast
+}  // namespace lg

@@ -1,0 +1,214 @@
+// lg_geometry.cuh -- hex-element geometry of the reference, generic in the
+// arithmetic type (double for the FP64 paths, float for the FP32 parts of the
+// mixed path).  Every expression keeps the reference's operand order; with
+// R = double the code is the reference's arithmetic operation for operation.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace lg {
+namespace geom {
+
+// ---------------------------------------------------------------------------
+// element geometry (lulesh.cc:290-474, 591-663, 1273-1435)
+// ---------------------------------------------------------------------------
+
+// Jacobian determinant of CalcElemShapeFunctionDerivatives (lulesh.cc:319-376)
+template <typename R>
+__device__ __forceinline__ R jacobian_det(const R *x, const R *y, const R *z)
+{
+    const R fjxxi = R(.125) * ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxet = R(.125) * ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxze = R(.125) * ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
+    const R fjyxi = R(.125) * ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyet = R(.125) * ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyze = R(.125) * ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
+    const R fjzxi = R(.125) * ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzet = R(.125) * ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzze = R(.125) * ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
+    const R cjxet = -(fjyxi * fjzze) + (fjzxi * fjyze);
+    const R cjyet = (fjxxi * fjzze) - (fjzxi * fjxze);
+    const R cjzet = -(fjxxi * fjyze) + (fjyxi * fjxze);
+    return R(8.) * (fjxet * cjxet + fjyet * cjyet + fjzet * cjzet);
+}
+
+// CalcElemShapeFunctionDerivatives rows 0..3 of B (rows 4..7 are their
+// negatives) and the determinant, lulesh.cc:290-377
+template <typename R>
+__device__ __forceinline__ R shape_derivs(const R *x, const R *y, const R *z, R bx[4], R by[4],
+                                          R bz[4])
+{
+    const R fjxxi = R(.125) * ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxet = R(.125) * ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxze = R(.125) * ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
+    const R fjyxi = R(.125) * ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyet = R(.125) * ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyze = R(.125) * ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
+    const R fjzxi = R(.125) * ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzet = R(.125) * ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzze = R(.125) * ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
+    const R cjxxi = (fjyet * fjzze) - (fjzet * fjyze);
+    const R cjxet = -(fjyxi * fjzze) + (fjzxi * fjyze);
+    const R cjxze = (fjyxi * fjzet) - (fjzxi * fjyet);
+    const R cjyxi = -(fjxet * fjzze) + (fjzet * fjxze);
+    const R cjyet = (fjxxi * fjzze) - (fjzxi * fjxze);
+    const R cjyze = -(fjxxi * fjzet) + (fjzxi * fjxet);
+    const R cjzxi = (fjxet * fjyze) - (fjyet * fjxze);
+    const R cjzet = -(fjxxi * fjyze) + (fjyxi * fjxze);
+    const R cjzze = (fjxxi * fjyet) - (fjyxi * fjxet);
+    bx[0] = -cjxxi - cjxet - cjxze;
+    bx[1] = cjxxi - cjxet - cjxze;
+    bx[2] = cjxxi + cjxet - cjxze;
+    bx[3] = -cjxxi + cjxet - cjxze;
+    by[0] = -cjyxi - cjyet - cjyze;
+    by[1] = cjyxi - cjyet - cjyze;
+    by[2] = cjyxi + cjyet - cjyze;
+    by[3] = -cjyxi + cjyet - cjyze;
+    bz[0] = -cjzxi - cjzet - cjzze;
+    bz[1] = cjzxi - cjzet - cjzze;
+    bz[2] = cjzxi + cjzet - cjzze;
+    bz[3] = -cjzxi + cjzet - cjzze;
+    return R(8.) * (fjxet * cjxet + fjyet * cjyet + fjzet * cjzet);
+}
+
+// SumElemFaceNormal, lulesh.cc:381-415 (the four corners a,b,c,d of a face)
+template <typename R>
+__device__ __forceinline__ void face_normal(R *nx, R *ny, R *nz, const R *x, const R *y,
+                                            const R *z, int a, int b, int c, int d)
+{
+    const R bisectX0 = R(0.5) * (x[d] + x[c] - x[b] - x[a]);
+    const R bisectY0 = R(0.5) * (y[d] + y[c] - y[b] - y[a]);
+    const R bisectZ0 = R(0.5) * (z[d] + z[c] - z[b] - z[a]);
+    const R bisectX1 = R(0.5) * (x[c] + x[b] - x[d] - x[a]);
+    const R bisectY1 = R(0.5) * (y[c] + y[b] - y[d] - y[a]);
+    const R bisectZ1 = R(0.5) * (z[c] + z[b] - z[d] - z[a]);
+    const R areaX = R(0.25) * (bisectY0 * bisectZ1 - bisectZ0 * bisectY1);
+    const R areaY = R(0.25) * (bisectZ0 * bisectX1 - bisectX0 * bisectZ1);
+    const R areaZ = R(0.25) * (bisectX0 * bisectY1 - bisectY0 * bisectX1);
+    nx[a] += areaX; nx[b] += areaX; nx[c] += areaX; nx[d] += areaX;
+    ny[a] += areaY; ny[b] += areaY; ny[c] += areaY; ny[d] += areaY;
+    nz[a] += areaZ; nz[b] += areaZ; nz[c] += areaZ; nz[d] += areaZ;
+}
+
+// CalcElemNodeNormals, lulesh.cc:419-474
+template <typename R>
+__device__ __forceinline__ void node_normals(R *pfx, R *pfy, R *pfz, const R *x, const R *y,
+                                             const R *z)
+{
+#pragma unroll
+    for (int i = 0; i < 8; ++i) pfx[i] = pfy[i] = pfz[i] = R(0.0);
+    face_normal(pfx, pfy, pfz, x, y, z, 0, 1, 2, 3);
+    face_normal(pfx, pfy, pfz, x, y, z, 0, 4, 5, 1);
+    face_normal(pfx, pfy, pfz, x, y, z, 1, 5, 6, 2);
+    face_normal(pfx, pfy, pfz, x, y, z, 2, 6, 7, 3);
+    face_normal(pfx, pfy, pfz, x, y, z, 3, 7, 4, 0);
+    face_normal(pfx, pfy, pfz, x, y, z, 4, 7, 6, 5);
+}
+
+// VoluDer, lulesh.cc:591-619, for corner k of CalcElemVolumeDerivative
+// (lulesh.cc:623-663) with neighbour nodes m0..m5
+template <typename R>
+__device__ __forceinline__ void volu_der(const R *x, const R *y, const R *z, int m0, int m1, int m2,
+                                         int m3, int m4, int m5, R &dvdx, R &dvdy, R &dvdz)
+{
+    const R twelfth = R(1.0) / R(12.0);
+    const R x0 = x[m0], x1 = x[m1], x2 = x[m2], x3 = x[m3], x4 = x[m4], x5 = x[m5];
+    const R y0 = y[m0], y1 = y[m1], y2 = y[m2], y3 = y[m3], y4 = y[m4], y5 = y[m5];
+    const R z0 = z[m0], z1 = z[m1], z2 = z[m2], z3 = z[m3], z4 = z[m4], z5 = z[m5];
+    dvdx = (y1 + y2) * (z0 + z1) - (y0 + y1) * (z1 + z2) + (y0 + y4) * (z3 + z4) -
+           (y3 + y4) * (z0 + z4) - (y2 + y5) * (z3 + z5) + (y3 + y5) * (z2 + z5);
+    dvdy = -(x1 + x2) * (z0 + z1) + (x0 + x1) * (z1 + z2) - (x0 + x4) * (z3 + z4) +
+           (x3 + x4) * (z0 + z4) + (x2 + x5) * (z3 + z5) - (x3 + x5) * (z2 + z5);
+    dvdz = -(y1 + y2) * (x0 + x1) + (y0 + y1) * (x1 + x2) - (y0 + y4) * (x3 + x4) +
+           (y3 + y4) * (x0 + x4) + (y2 + y5) * (x3 + x5) - (y3 + y5) * (x2 + x5);
+    dvdx *= twelfth;
+    dvdy *= twelfth;
+    dvdz *= twelfth;
+}
+
+template <typename R>
+__device__ __forceinline__ void volume_derivative(const R *x, const R *y, const R *z, R *dvdx,
+                                                  R *dvdy, R *dvdz)
+{
+    volu_der(x, y, z, 1, 2, 3, 4, 5, 7, dvdx[0], dvdy[0], dvdz[0]);
+    volu_der(x, y, z, 0, 1, 2, 7, 4, 6, dvdx[3], dvdy[3], dvdz[3]);
+    volu_der(x, y, z, 3, 0, 1, 6, 7, 5, dvdx[2], dvdy[2], dvdz[2]);
+    volu_der(x, y, z, 2, 3, 0, 5, 6, 4, dvdx[1], dvdy[1], dvdz[1]);
+    volu_der(x, y, z, 7, 6, 5, 0, 3, 1, dvdx[4], dvdy[4], dvdz[4]);
+    volu_der(x, y, z, 4, 7, 6, 1, 0, 2, dvdx[5], dvdy[5], dvdz[5]);
+    volu_der(x, y, z, 5, 4, 7, 2, 1, 3, dvdx[6], dvdy[6], dvdz[6]);
+    volu_der(x, y, z, 6, 5, 4, 3, 2, 0, dvdx[7], dvdy[7], dvdz[7]);
+}
+
+// CalcElemVolume, lulesh.cc:1273-1356
+template <typename R>
+__device__ __forceinline__ R elem_volume(const R *x, const R *y, const R *z)
+{
+    const R twelveth = R(1.0) / R(12.0);
+    const R dx61 = x[6] - x[1], dy61 = y[6] - y[1], dz61 = z[6] - z[1];
+    const R dx70 = x[7] - x[0], dy70 = y[7] - y[0], dz70 = z[7] - z[0];
+    const R dx63 = x[6] - x[3], dy63 = y[6] - y[3], dz63 = z[6] - z[3];
+    const R dx20 = x[2] - x[0], dy20 = y[2] - y[0], dz20 = z[2] - z[0];
+    const R dx50 = x[5] - x[0], dy50 = y[5] - y[0], dz50 = z[5] - z[0];
+    const R dx64 = x[6] - x[4], dy64 = y[6] - y[4], dz64 = z[6] - z[4];
+    const R dx31 = x[3] - x[1], dy31 = y[3] - y[1], dz31 = z[3] - z[1];
+    const R dx72 = x[7] - x[2], dy72 = y[7] - y[2], dz72 = z[7] - z[2];
+    const R dx43 = x[4] - x[3], dy43 = y[4] - y[3], dz43 = z[4] - z[3];
+    const R dx57 = x[5] - x[7], dy57 = y[5] - y[7], dz57 = z[5] - z[7];
+    const R dx14 = x[1] - x[4], dy14 = y[1] - y[4], dz14 = z[1] - z[4];
+    const R dx25 = x[2] - x[5], dy25 = y[2] - y[5], dz25 = z[2] - z[5];
+#define LG_TP(a1, b1, c1, a2, b2, c2, a3, b3, c3) \
+    ((a1) * ((b2) * (c3) - (c2) * (b3)) + (a2) * ((c1) * (b3) - (b1) * (c3)) + \
+     (a3) * ((b1) * (c2) - (c1) * (b2)))
+    R volume =
+        LG_TP(dx31 + dx72, dx63, dx20, dy31 + dy72, dy63, dy20, dz31 + dz72, dz63, dz20) +
+        LG_TP(dx43 + dx57, dx64, dx70, dy43 + dy57, dy64, dy70, dz43 + dz57, dz64, dz70) +
+        LG_TP(dx14 + dx25, dx61, dx50, dy14 + dy25, dy61, dy50, dz14 + dz25, dz61, dz50);
+#undef LG_TP
+    volume *= twelveth;
+    return volume;
+}
+
+// AreaFace, lulesh.cc:1370-1390
+template <typename R>
+__device__ __forceinline__ R area_face(const R *x, const R *y, const R *z, int a, int b, int c,
+                                       int d)
+{
+    const R fx = (x[c] - x[a]) - (x[d] - x[b]);
+    const R fy = (y[c] - y[a]) - (y[d] - y[b]);
+    const R fz = (z[c] - z[a]) - (z[d] - z[b]);
+    const R gx = (x[c] - x[a]) + (x[d] - x[b]);
+    const R gy = (y[c] - y[a]) + (y[d] - y[b]);
+    const R gz = (z[c] - z[a]) + (z[d] - z[b]);
+    return (fx * fx + fy * fy + fz * fz) * (gx * gx + gy * gy + gz * gz) -
+           (fx * gx + fy * gy + fz * gz) * (fx * gx + fy * gy + fz * gz);
+}
+
+// CalcElemCharacteristicLength, lulesh.cc:1394-1435 (std::max(a,b) is
+// (a < b) ? b : a)
+template <typename R>
+__device__ __forceinline__ R char_length(const R *x, const R *y, const R *z, R volume)
+{
+    R cl = R(0.0), a;
+    a = area_face(x, y, z, 0, 1, 2, 3); cl = (a < cl) ? cl : a;
+    a = area_face(x, y, z, 4, 5, 6, 7); cl = (a < cl) ? cl : a;
+    a = area_face(x, y, z, 0, 1, 5, 4); cl = (a < cl) ? cl : a;
+    a = area_face(x, y, z, 1, 2, 6, 5); cl = (a < cl) ? cl : a;
+    a = area_face(x, y, z, 2, 3, 7, 6); cl = (a < cl) ? cl : a;
+    a = area_face(x, y, z, 3, 0, 4, 7); cl = (a < cl) ? cl : a;
+    return R(4.0) * volume / sqrt(cl);
+}
+
+// hourglass base vectors, lulesh.cc:743-776
+template <typename R = double>
+__device__ __forceinline__ constexpr R gam(int mode, int k)
+{
+    constexpr signed char G[4][8] = {{1, 1, -1, -1, -1, -1, 1, 1},
+                                     {1, -1, -1, 1, -1, 1, 1, -1},
+                                     {1, -1, 1, -1, 1, -1, 1, -1},
+                                     {-1, 1, -1, 1, 1, -1, 1, -1}};
+    return (R)G[mode][k];
+}
+
+}  // namespace geom
+}  // namespace lg

@@ -30,6 +30,8 @@
 #include <cstdint>
 
 #include "lg_device.h"
+#include "lg_geometry.cuh"
+#include "lg_cycle_common.cuh"
 
 #ifndef LG_NS
 #error "define LG_NS"
@@ -38,258 +40,8 @@
 namespace lg {
 namespace LG_NS {
 
-constexpr int kBlock = 128;
-
-// Keeps the compiler from treating a value as loop-invariant, so that every
-// EOS repetition the reference performs is evaluated.
-__device__ __forceinline__ void opaque(double &v) { asm volatile("" : "+d"(v)); }
-
-__device__ __forceinline__ void raise_status(Ctl *c, int code) { atomicCAS(&c->status, 0, code); }
-
-// TimeIncrement, lulesh.cc:166-222
-__device__ __forceinline__ void time_increment(Ctl *c)
-{
-    double targetdt = c->stoptime - c->time;
-    if ((c->dtfixed <= 0.0) && (c->cycle != 0)) {
-        double ratio;
-        const double olddt = c->deltatime;
-        double gnewdt = 1.0e+20;
-        double newdt;
-        if (c->dtcourant < gnewdt) gnewdt = c->dtcourant / 2.0;
-        if (c->dthydro < gnewdt) gnewdt = c->dthydro * 2.0 / 3.0;
-        newdt = gnewdt;
-        ratio = newdt / olddt;
-        if (ratio >= 1.0) {
-            if (ratio < c->dtmultlb)
-                newdt = olddt;
-            else if (ratio > c->dtmultub)
-                newdt = olddt * c->dtmultub;
-        }
-        if (newdt > c->dtmax) newdt = c->dtmax;
-        c->deltatime = newdt;
-    }
-    if ((targetdt > c->deltatime) && (targetdt < (4.0 * c->deltatime / 3.0)))
-        targetdt = 2.0 * c->deltatime / 3.0;
-    if (targetdt < c->deltatime) c->deltatime = targetdt;
-    c->time += c->deltatime;
-    ++c->cycle;
-}
-
-// Loop condition of lulesh.cc:2745 followed by TimeIncrement.
-__device__ __forceinline__ void begin_cycle(Ctl *c)
-{
-    if (c->status == 0 && c->time < c->stoptime && c->cycle < c->cycle_limit) {
-        time_increment(c);
-        c->active = 1;
-    } else {
-        c->active = 0;
-    }
-}
-
-__global__ void k_begin(Ctl *c) { begin_cycle(c); }
-__global__ void k_time_increment(Ctl *c)
-{
-    time_increment(c);
-    c->active = 1;
-}
-__global__ void k_set_active(Ctl *c) { c->active = 1; }
-
-__device__ __forceinline__ bool cycle_live(const Ctl *c) { return c->active && c->status == 0; }
-
-// ---------------------------------------------------------------------------
-// element geometry (lulesh.cc:290-474, 591-663, 1273-1435)
-// ---------------------------------------------------------------------------
-
-// Jacobian determinant of CalcElemShapeFunctionDerivatives (lulesh.cc:319-376)
-__device__ __forceinline__ double jacobian_det(const double *x, const double *y, const double *z)
-{
-    const double fjxxi = .125 * ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
-    const double fjxet = .125 * ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
-    const double fjxze = .125 * ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
-    const double fjyxi = .125 * ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
-    const double fjyet = .125 * ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
-    const double fjyze = .125 * ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
-    const double fjzxi = .125 * ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
-    const double fjzet = .125 * ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
-    const double fjzze = .125 * ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
-    const double cjxet = -(fjyxi * fjzze) + (fjzxi * fjyze);
-    const double cjyet = (fjxxi * fjzze) - (fjzxi * fjxze);
-    const double cjzet = -(fjxxi * fjyze) + (fjyxi * fjxze);
-    return 8. * (fjxet * cjxet + fjyet * cjyet + fjzet * cjzet);
-}
-
-// CalcElemShapeFunctionDerivatives rows 0..3 of B (rows 4..7 are their
-// negatives) and the determinant, lulesh.cc:290-377
-__device__ __forceinline__ double shape_derivs(const double *x, const double *y, const double *z,
-                                               double bx[4], double by[4], double bz[4])
-{
-    const double fjxxi = .125 * ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
-    const double fjxet = .125 * ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
-    const double fjxze = .125 * ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
-    const double fjyxi = .125 * ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
-    const double fjyet = .125 * ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
-    const double fjyze = .125 * ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
-    const double fjzxi = .125 * ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
-    const double fjzet = .125 * ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
-    const double fjzze = .125 * ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
-    const double cjxxi = (fjyet * fjzze) - (fjzet * fjyze);
-    const double cjxet = -(fjyxi * fjzze) + (fjzxi * fjyze);
-    const double cjxze = (fjyxi * fjzet) - (fjzxi * fjyet);
-    const double cjyxi = -(fjxet * fjzze) + (fjzet * fjxze);
-    const double cjyet = (fjxxi * fjzze) - (fjzxi * fjxze);
-    const double cjyze = -(fjxxi * fjzet) + (fjzxi * fjxet);
-    const double cjzxi = (fjxet * fjyze) - (fjyet * fjxze);
-    const double cjzet = -(fjxxi * fjyze) + (fjyxi * fjxze);
-    const double cjzze = (fjxxi * fjyet) - (fjyxi * fjxet);
-    bx[0] = -cjxxi - cjxet - cjxze;
-    bx[1] = cjxxi - cjxet - cjxze;
-    bx[2] = cjxxi + cjxet - cjxze;
-    bx[3] = -cjxxi + cjxet - cjxze;
-    by[0] = -cjyxi - cjyet - cjyze;
-    by[1] = cjyxi - cjyet - cjyze;
-    by[2] = cjyxi + cjyet - cjyze;
-    by[3] = -cjyxi + cjyet - cjyze;
-    bz[0] = -cjzxi - cjzet - cjzze;
-    bz[1] = cjzxi - cjzet - cjzze;
-    bz[2] = cjzxi + cjzet - cjzze;
-    bz[3] = -cjzxi + cjzet - cjzze;
-    return 8. * (fjxet * cjxet + fjyet * cjyet + fjzet * cjzet);
-}
-
-// SumElemFaceNormal, lulesh.cc:381-415 (the four corners a,b,c,d of a face)
-__device__ __forceinline__ void face_normal(double *nx, double *ny, double *nz, const double *x,
-                                            const double *y, const double *z, int a, int b, int c,
-                                            int d)
-{
-    const double bisectX0 = 0.5 * (x[d] + x[c] - x[b] - x[a]);
-    const double bisectY0 = 0.5 * (y[d] + y[c] - y[b] - y[a]);
-    const double bisectZ0 = 0.5 * (z[d] + z[c] - z[b] - z[a]);
-    const double bisectX1 = 0.5 * (x[c] + x[b] - x[d] - x[a]);
-    const double bisectY1 = 0.5 * (y[c] + y[b] - y[d] - y[a]);
-    const double bisectZ1 = 0.5 * (z[c] + z[b] - z[d] - z[a]);
-    const double areaX = 0.25 * (bisectY0 * bisectZ1 - bisectZ0 * bisectY1);
-    const double areaY = 0.25 * (bisectZ0 * bisectX1 - bisectX0 * bisectZ1);
-    const double areaZ = 0.25 * (bisectX0 * bisectY1 - bisectY0 * bisectX1);
-    nx[a] += areaX; nx[b] += areaX; nx[c] += areaX; nx[d] += areaX;
-    ny[a] += areaY; ny[b] += areaY; ny[c] += areaY; ny[d] += areaY;
-    nz[a] += areaZ; nz[b] += areaZ; nz[c] += areaZ; nz[d] += areaZ;
-}
-
-// CalcElemNodeNormals, lulesh.cc:419-474
-__device__ __forceinline__ void node_normals(double *pfx, double *pfy, double *pfz,
-                                             const double *x, const double *y, const double *z)
-{
-#pragma unroll
-    for (int i = 0; i < 8; ++i) pfx[i] = pfy[i] = pfz[i] = 0.0;
-    face_normal(pfx, pfy, pfz, x, y, z, 0, 1, 2, 3);
-    face_normal(pfx, pfy, pfz, x, y, z, 0, 4, 5, 1);
-    face_normal(pfx, pfy, pfz, x, y, z, 1, 5, 6, 2);
-    face_normal(pfx, pfy, pfz, x, y, z, 2, 6, 7, 3);
-    face_normal(pfx, pfy, pfz, x, y, z, 3, 7, 4, 0);
-    face_normal(pfx, pfy, pfz, x, y, z, 4, 7, 6, 5);
-}
-
-// VoluDer, lulesh.cc:591-619, for corner k of CalcElemVolumeDerivative
-// (lulesh.cc:623-663) with neighbour nodes m0..m5
-__device__ __forceinline__ void volu_der(const double *x, const double *y, const double *z, int m0,
-                                         int m1, int m2, int m3, int m4, int m5, double &dvdx,
-                                         double &dvdy, double &dvdz)
-{
-    const double twelfth = 1.0 / 12.0;
-    const double x0 = x[m0], x1 = x[m1], x2 = x[m2], x3 = x[m3], x4 = x[m4], x5 = x[m5];
-    const double y0 = y[m0], y1 = y[m1], y2 = y[m2], y3 = y[m3], y4 = y[m4], y5 = y[m5];
-    const double z0 = z[m0], z1 = z[m1], z2 = z[m2], z3 = z[m3], z4 = z[m4], z5 = z[m5];
-    dvdx = (y1 + y2) * (z0 + z1) - (y0 + y1) * (z1 + z2) + (y0 + y4) * (z3 + z4) -
-           (y3 + y4) * (z0 + z4) - (y2 + y5) * (z3 + z5) + (y3 + y5) * (z2 + z5);
-    dvdy = -(x1 + x2) * (z0 + z1) + (x0 + x1) * (z1 + z2) - (x0 + x4) * (z3 + z4) +
-           (x3 + x4) * (z0 + z4) + (x2 + x5) * (z3 + z5) - (x3 + x5) * (z2 + z5);
-    dvdz = -(y1 + y2) * (x0 + x1) + (y0 + y1) * (x1 + x2) - (y0 + y4) * (x3 + x4) +
-           (y3 + y4) * (x0 + x4) + (y2 + y5) * (x3 + x5) - (y3 + y5) * (x2 + x5);
-    dvdx *= twelfth;
-    dvdy *= twelfth;
-    dvdz *= twelfth;
-}
-
-__device__ __forceinline__ void volume_derivative(const double *x, const double *y,
-                                                  const double *z, double *dvdx, double *dvdy,
-                                                  double *dvdz)
-{
-    volu_der(x, y, z, 1, 2, 3, 4, 5, 7, dvdx[0], dvdy[0], dvdz[0]);
-    volu_der(x, y, z, 0, 1, 2, 7, 4, 6, dvdx[3], dvdy[3], dvdz[3]);
-    volu_der(x, y, z, 3, 0, 1, 6, 7, 5, dvdx[2], dvdy[2], dvdz[2]);
-    volu_der(x, y, z, 2, 3, 0, 5, 6, 4, dvdx[1], dvdy[1], dvdz[1]);
-    volu_der(x, y, z, 7, 6, 5, 0, 3, 1, dvdx[4], dvdy[4], dvdz[4]);
-    volu_der(x, y, z, 4, 7, 6, 1, 0, 2, dvdx[5], dvdy[5], dvdz[5]);
-    volu_der(x, y, z, 5, 4, 7, 2, 1, 3, dvdx[6], dvdy[6], dvdz[6]);
-    volu_der(x, y, z, 6, 5, 4, 3, 2, 0, dvdx[7], dvdy[7], dvdz[7]);
-}
-
-// CalcElemVolume, lulesh.cc:1273-1356
-__device__ __forceinline__ double elem_volume(const double *x, const double *y, const double *z)
-{
-    const double twelveth = 1.0 / 12.0;
-    const double dx61 = x[6] - x[1], dy61 = y[6] - y[1], dz61 = z[6] - z[1];
-    const double dx70 = x[7] - x[0], dy70 = y[7] - y[0], dz70 = z[7] - z[0];
-    const double dx63 = x[6] - x[3], dy63 = y[6] - y[3], dz63 = z[6] - z[3];
-    const double dx20 = x[2] - x[0], dy20 = y[2] - y[0], dz20 = z[2] - z[0];
-    const double dx50 = x[5] - x[0], dy50 = y[5] - y[0], dz50 = z[5] - z[0];
-    const double dx64 = x[6] - x[4], dy64 = y[6] - y[4], dz64 = z[6] - z[4];
-    const double dx31 = x[3] - x[1], dy31 = y[3] - y[1], dz31 = z[3] - z[1];
-    const double dx72 = x[7] - x[2], dy72 = y[7] - y[2], dz72 = z[7] - z[2];
-    const double dx43 = x[4] - x[3], dy43 = y[4] - y[3], dz43 = z[4] - z[3];
-    const double dx57 = x[5] - x[7], dy57 = y[5] - y[7], dz57 = z[5] - z[7];
-    const double dx14 = x[1] - x[4], dy14 = y[1] - y[4], dz14 = z[1] - z[4];
-    const double dx25 = x[2] - x[5], dy25 = y[2] - y[5], dz25 = z[2] - z[5];
-#define LG_TP(a1, b1, c1, a2, b2, c2, a3, b3, c3) \
-    ((a1) * ((b2) * (c3) - (c2) * (b3)) + (a2) * ((c1) * (b3) - (b1) * (c3)) + \
-     (a3) * ((b1) * (c2) - (c1) * (b2)))
-    double volume =
-        LG_TP(dx31 + dx72, dx63, dx20, dy31 + dy72, dy63, dy20, dz31 + dz72, dz63, dz20) +
-        LG_TP(dx43 + dx57, dx64, dx70, dy43 + dy57, dy64, dy70, dz43 + dz57, dz64, dz70) +
-        LG_TP(dx14 + dx25, dx61, dx50, dy14 + dy25, dy61, dy50, dz14 + dz25, dz61, dz50);
-#undef LG_TP
-    volume *= twelveth;
-    return volume;
-}
-
-// AreaFace, lulesh.cc:1370-1390
-__device__ __forceinline__ double area_face(const double *x, const double *y, const double *z,
-                                            int a, int b, int c, int d)
-{
-    const double fx = (x[c] - x[a]) - (x[d] - x[b]);
-    const double fy = (y[c] - y[a]) - (y[d] - y[b]);
-    const double fz = (z[c] - z[a]) - (z[d] - z[b]);
-    const double gx = (x[c] - x[a]) + (x[d] - x[b]);
-    const double gy = (y[c] - y[a]) + (y[d] - y[b]);
-    const double gz = (z[c] - z[a]) + (z[d] - z[b]);
-    return (fx * fx + fy * fy + fz * fz) * (gx * gx + gy * gy + gz * gz) -
-           (fx * gx + fy * gy + fz * gz) * (fx * gx + fy * gy + fz * gz);
-}
-
-// CalcElemCharacteristicLength, lulesh.cc:1394-1435 (std::max(a,b) is
-// (a < b) ? b : a)
-__device__ __forceinline__ double char_length(const double *x, const double *y, const double *z,
-                                              double volume)
-{
-    double cl = 0.0, a;
-    a = area_face(x, y, z, 0, 1, 2, 3); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 4, 5, 6, 7); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 0, 1, 5, 4); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 1, 2, 6, 5); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 2, 3, 7, 6); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 3, 0, 4, 7); cl = (a < cl) ? cl : a;
-    return 4.0 * volume / sqrt(cl);
-}
-
-// hourglass base vectors, lulesh.cc:743-776
-__device__ __forceinline__ constexpr double gam(int mode, int k)
-{
-    constexpr signed char G[4][8] = {{1, 1, -1, -1, -1, -1, 1, 1},
-                                     {1, -1, -1, 1, -1, 1, 1, -1},
-                                     {1, -1, 1, -1, 1, -1, 1, -1},
-                                     {-1, 1, -1, 1, 1, -1, 1, -1}};
-    return (double)G[mode][k];
-}
+// element geometry: lg_geometry.cuh
+using namespace ::lg::geom;
 
 // ---------------------------------------------------------------------------
 // k_forces: CalcVolumeForceForElems (lulesh.cc:1062-1100)
@@ -555,217 +307,6 @@ __global__ void __launch_bounds__(kBlock) k_kinematics(DevState s)
 #undef S4
 }
 
-// ---------------------------------------------------------------------------
-// k_material
-// ---------------------------------------------------------------------------
-
-// one direction of CalcMonotonicQRegionForElems, lulesh.cc:1778-1813
-__device__ __forceinline__ double monoq_phi(const Params &P, const double *dv, int ielem, int bc,
-                                            int msymm, int mfree, int mmask, int psymm,
-                                            int pfree, int pmask, int nbm, int nbp)
-{
-    const double ptiny = 1.e-36;
-    double delvm, delvp;
-    const double self = dv[ielem];
-    const double norm = 1. / (self + ptiny);
-    const int bm = bc & mmask, bp = bc & pmask;
-    if (bm == msymm)
-        delvm = self;
-    else if (bm == mfree)
-        delvm = 0.0;
-    else if (bm == 0 || bm == (mmask & ~(msymm | mfree)))
-        delvm = dv[nbm];
-    else
-        delvm = 0;
-    if (bp == psymm)
-        delvp = self;
-    else if (bp == pfree)
-        delvp = 0.0;
-    else if (bp == 0 || bp == (pmask & ~(psymm | pfree)))
-        delvp = dv[nbp];
-    else
-        delvp = 0;
-    delvm = delvm * norm;
-    delvp = delvp * norm;
-    double phi = .5 * (delvm + delvp);
-    delvm *= P.monoq_limiter_mult;
-    delvp *= P.monoq_limiter_mult;
-    if (delvm < phi) phi = delvm;
-    if (delvp < phi) phi = delvp;
-    if (phi < 0.) phi = 0.;
-    if (phi > P.monoq_max_slope) phi = P.monoq_max_slope;
-    return phi;
-}
-
-// sound-speed term of lulesh.cc:2083-2090, 2126-2133, 2158-2165, 2190-2197
-__device__ __forceinline__ double ssc_of(double num, double rho0)
-{
-    double ssc = (rho0 == 1.0) ? num : num / rho0;
-    if (ssc <= .1111111e-36)
-        ssc = .3333333e-18;
-    else
-        ssc = sqrt(ssc);
-    return ssc;
-}
-
-// CalcPressureForElems for one element, lulesh.cc:2014-2044
-__device__ __forceinline__ double pressure(const Params &P, double &bvc, double &pbvc,
-                                           double e_old, double compression, double vnewc)
-{
-    const double c1s = 2.0 / 3.0;
-    bvc = c1s * (compression + 1.);
-    pbvc = c1s;
-    double p_new = bvc * e_old;
-    if (fabs(p_new) < P.p_cut) p_new = 0.0;
-    if (vnewc >= P.eosvmax) p_new = 0.0;
-    if (p_new < P.pmin) p_new = P.pmin;
-    return p_new;
-}
-
-// EvalEOSForElems for one element (lulesh.cc:2204-2324) with
-// CalcEnergyForElems (2048-2176) and CalcSoundSpeedForElems (2180-2200).
-// All rep repetitions are evaluated, as in the reference.
-__device__ __forceinline__ void eval_eos(const Params &P, double e_in, double delv_in,
-                                         double p_in, double q_in, double qq_in, double ql_in,
-                                         double vnewc, int rep, double &p_out, double &e_out,
-                                         double &q_out, double &ss_out)
-{
-    const double rho0 = P.refdens;
-    double p_new = 0., e_new = 0., q_new = 0., bvc = 0., pbvc = 0.;
-    for (int j = 0; j < rep; j++) {
-        double e_old = e_in, delvc = delv_in, p_old = p_in, q_old = q_in, qq_old = qq_in,
-               ql_old = ql_in, vc = vnewc;
-        opaque(e_old); opaque(delvc); opaque(p_old); opaque(q_old);
-        opaque(qq_old); opaque(ql_old); opaque(vc);
-        double compression = 1. / vc - 1.;
-        const double vchalf = vc - delvc * .5;
-        double compHalfStep = 1. / vchalf - 1.;
-        if (P.eosvmin != 0. && vc <= P.eosvmin) compHalfStep = compression;
-        if (P.eosvmax != 0. && vc >= P.eosvmax) {
-            p_old = 0.;
-            compression = 0.;
-            compHalfStep = 0.;
-        }
-        const double work = 0.;
-
-        e_new = e_old - .5 * delvc * (p_old + q_old) + .5 * work;
-        if (e_new < P.emin) e_new = P.emin;
-
-        const double pHalfStep = pressure(P, bvc, pbvc, e_new, compHalfStep, vc);
-        const double vhalf = 1. / (1. + compHalfStep);
-        if (delvc > 0.) {
-            q_new = 0.;
-        } else {
-            const double ssc = ssc_of(pbvc * e_new + vhalf * vhalf * bvc * pHalfStep, rho0);
-            q_new = (ssc * ql_old + qq_old);
-        }
-        e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (pHalfStep + q_new));
-
-        e_new += .5 * work;
-        if (fabs(e_new) < P.e_cut) e_new = 0.;
-        if (e_new < P.emin) e_new = P.emin;
-
-        p_new = pressure(P, bvc, pbvc, e_new, compression, vc);
-        {
-            const double sixth = 1.0 / 6.0;
-            double q_tilde;
-            if (delvc > 0.) {
-                q_tilde = 0.;
-            } else {
-                const double ssc = ssc_of(pbvc * e_new + vc * vc * bvc * p_new, rho0);
-                q_tilde = (ssc * ql_old + qq_old);
-            }
-            e_new = e_new - (7.0 * (p_old + q_old) - 8.0 * (pHalfStep + q_new) +
-                             (p_new + q_tilde)) * delvc * sixth;
-            if (fabs(e_new) < P.e_cut) e_new = 0.;
-            if (e_new < P.emin) e_new = P.emin;
-        }
-
-        p_new = pressure(P, bvc, pbvc, e_new, compression, vc);
-        if (delvc <= 0.) {
-            const double ssc = ssc_of(pbvc * e_new + vc * vc * bvc * p_new, rho0);
-            q_new = (ssc * ql_old + qq_old);
-            if (fabs(q_new) < P.q_cut) q_new = 0.;
-        }
-    }
-    p_out = p_new;
-    e_out = e_new;
-    q_out = q_new;
-    ss_out = ssc_of(pbvc * e_new + vnewc * vnewc * bvc * p_new, rho0);
-}
-
-__device__ __forceinline__ double dmin_sel(double a, double b) { return (b < a) ? b : a; }
-
-// Reduces (dtc, dth) over the block; the last block of the grid reduces the
-// per-block results into ctl->dtcourant/dthydro, merges error flags and, if
-// advance, evaluates the loop condition and TimeIncrement of the next cycle.
-__device__ __forceinline__ void finish_dt(DevState &s, double dtc, double dth, bool advance)
-{
-    __shared__ double red[2][kBlock / 32];
-    __shared__ bool am_last;
-    Ctl *ctl = s.ctl;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        dtc = dmin_sel(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-        dth = dmin_sel(dth, __shfl_down_sync(0xffffffffu, dth, off));
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        red[0][warp] = dtc;
-        red[1][warp] = dth;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double bc = red[0][0], bh = red[1][0];
-        for (int w = 1; w < kBlock / 32; ++w) {
-            bc = dmin_sel(bc, red[0][w]);
-            bh = dmin_sel(bh, red[1][w]);
-        }
-        s.dt_partial[2 * blockIdx.x] = bc;
-        s.dt_partial[2 * blockIdx.x + 1] = bh;
-        __threadfence();
-        const unsigned prev = atomicAdd(&ctl->blocks_done, 1u);
-        am_last = (prev == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!am_last) return;
-    __threadfence();
-    double c = 1.0e+20, h = 1.0e+20;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-        c = dmin_sel(c, __ldcg(&s.dt_partial[2 * i]));
-        h = dmin_sel(h, __ldcg(&s.dt_partial[2 * i + 1]));
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        c = dmin_sel(c, __shfl_down_sync(0xffffffffu, c, off));
-        h = dmin_sel(h, __shfl_down_sync(0xffffffffu, h, off));
-    }
-    __syncthreads();
-    if (lane == 0) {
-        red[0][warp] = c;
-        red[1][warp] = h;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < kBlock / 32; ++w) {
-            red[0][0] = dmin_sel(red[0][0], red[0][w]);
-            red[1][0] = dmin_sel(red[1][0], red[1][w]);
-        }
-        ctl->dtcourant = red[0][0];
-        ctl->dthydro = red[1][0];
-        ctl->blocks_done = 0;
-        if (ctl->status == 0) {
-            if (ctl->err_qstop)
-                ctl->status = -2;
-            else if (ctl->err_matvol)
-                ctl->status = -1;
-        }
-        ctl->err_qstop = 0;
-        ctl->err_matvol = 0;
-        if (advance) begin_cycle(ctl);
-    }
-}
-
 // MODE 0: Q limiter + qstop + EOS + sound speed + volume update (the part of
 //         LagrangeElements after the kinematics)
 // MODE 1: time constraints only (CalcTimeConstraintsForElems)
@@ -784,13 +325,13 @@ __global__ void __launch_bounds__(kBlock) k_material(DevState s)
         if (MODE != 1) {
             // CalcMonotonicQRegionForElems, lulesh.cc:1761-1921
             const int bc = s.elemBC[ielem];
-            const double phixi = monoq_phi(P, s.delv_xi, ielem, bc, XI_M_SYMM, XI_M_FREE,
+            const double phixi = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_xi, ielem, bc, XI_M_SYMM, XI_M_FREE,
                                            XI_M, XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
                                            s.lxip[ielem]);
-            const double phieta = monoq_phi(P, s.delv_eta, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
+            const double phieta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_eta, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
                                             ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P,
                                             s.letam[ielem], s.letap[ielem]);
-            const double phizeta = monoq_phi(P, s.delv_zeta, ielem, bc, ZETA_M_SYMM,
+            const double phizeta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_zeta, ielem, bc, ZETA_M_SYMM,
                                              ZETA_M_FREE, ZETA_M, ZETA_P_SYMM, ZETA_P_FREE,
                                              ZETA_P, s.lzetam[ielem], s.lzetap[ielem]);
             const double vnew = s.vnew[ielem];

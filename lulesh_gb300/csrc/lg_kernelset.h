@@ -26,5 +26,6 @@ struct KernelSet {
 
 const KernelSet *kernels_fp64_strict();
 const KernelSet *kernels_fp64_fma();
+const KernelSet *kernels_mixed();
 
 }  // namespace lg
