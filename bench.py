@@ -229,6 +229,106 @@ def d_device(d) -> int:
     return int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def run_ensemble(a):
+    """The batched ensemble (BASELINE config 4) against the plain path run
+    member by member, same members, same precision, same cycles."""
+    dist, ws, rank, local = _dist()
+    import numpy as np
+    import lulesh_gb300 as lg
+    members = lg.sample_ensemble(a.ensemble, seed=a.seed)
+    for m in members:
+        m["its"] = 10 ** 9
+    en = lg.Ensemble(members, precision=a.precision, device=local)
+    info = en.info()
+    E = info["elements"]
+    tune = en.autotune(3)
+    if a.warmup:
+        en.step(a.warmup)
+    en.reset()
+    l0 = en.info()["launches"]
+    _barrier(dist)
+    with ClockSampler(local) as clk:
+        st, ms = en.step_timed(a.steps)
+        _barrier(dist)
+    launches = en.info()["launches"] - l0
+    if st != 0:
+        raise SystemExit(f"ensemble run failed with status {st}")
+    ms_max = _max_over_ranks(dist, ms)
+    value = ws * E * a.steps / (ms_max * 1e3)
+
+    # end to end through the C ABI: upload every member from host memory,
+    # the K cycles, download every member's fields
+    fields = lg.NODE_FIELDS + lg.ELEM_FIELDS
+    t0 = time.perf_counter()
+    en.reset()
+    en.step(a.steps)
+    d2h = 0
+    for i in range(len(members)):
+        for f in fields:
+            d2h += en.field(i, f).nbytes
+    t_e2e = _max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": ws * E * a.steps / (t_e2e * 1e6), "unit": UNIT,
+           "h2d_bytes_per_step": d2h / a.steps, "d2h_bytes_per_step": d2h / a.steps}
+
+    # the plain path, member by member (device time of each member's cycles)
+    seq_ms = 0.0
+    for m in members:
+        d = lg.Domain(m["nx"], m["numReg"], m["balance"], m["cost"], its=10 ** 9,
+                      hgcoef=m["hgcoef"], einit_factor=m["einit_factor"],
+                      precision=a.precision, device=local)
+        d.step(min(a.warmup, 2))
+        d.reset()
+        _, t = d.step_timed(a.steps)
+        seq_ms += t
+        d.close()
+    seq_value = E * a.steps / (seq_ms * 1e3)
+    sizes = [m["nx"] for m in members]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if a.precision != "mixed" else "f64+f32",
+            "data": "synthetic: the reference's Sedov set-up for every member",
+            "config": {"workload": f"ensemble of {len(members)} Sedov problems (seed {a.seed}): "
+                                   f"s in {min(sizes)}..{max(sizes)}, {E} elements in all, "
+                                   f"{a.steps} cycles, {a.precision}",
+                       "members": len(members), "elements": E, "cycles": a.steps,
+                       "precision": a.precision, "seed": a.seed,
+                       "l2": "inputs larger than L2", "parallelism": "replicas"},
+            "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+            "sequential_plain": {"value": seq_value, "unit": UNIT,
+                                 "how": "each member alone through lg_create/lg_step_timed"},
+            "batched_over_sequential": value / seq_value, "autotune": tune}
+    if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_ensemble_rate(members, float(
+            os.environ.get("LG_CPU_BUDGET_S", "15")))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cpu_ensemble_rate(members, budget_s: float) -> dict:
+    """The reference algorithm (oracle port) on the members one after another."""
+    from oracle import oracle
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    done_ec, t, ran = 0, 0.0, 0
+    for m in members:
+        if t >= budget_s:
+            break
+        o = oracle.OracleDomain(m["nx"], m["numReg"], m["balance"], m["cost"], m["hgcoef"],
+                                m["einit_factor"], fast=True)
+        c = 0
+        while c < 300 and t < budget_s:
+            t1 = time.perf_counter()
+            o.step(1)
+            t += time.perf_counter() - t1
+            c += 1
+        done_ec += c * m["nx"] ** 3
+        ran += 1
+        o.close()
+    return {"value": done_ec / (t * 1e6) if t else 0.0, "unit": UNIT, "cores": threads,
+            "kind": "port", "sample": f"the first {ran} members in order, up to 300 cycles each, "
+                                      f"{t:.1f} s timed; oracle C restatement, {threads} threads"}
+
+
 def run_reference(a):
     dist, ws, rank, local = _dist()
     if rank != 0:
@@ -349,7 +449,8 @@ def run_gpu(a):
 def main():
     p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=500)
+    p.add_argument("--steps", type=int, default=None,
+                   help="cycles to time (default 500; 300 with --ensemble)")
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--nx", type=int, default=150)
@@ -358,15 +459,22 @@ def main():
     p.add_argument("--cost", type=int, default=1)
     p.add_argument("--precision", default="fp64", choices=["fp64", "fp64-fma", "mixed"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--ensemble", type=int, default=0,
+                   help="batched ensemble of this many sampled problems instead of one problem")
+    p.add_argument("--seed", type=int, default=0, help="ensemble sample seed")
     p.add_argument("--err-vs-fp64", action="store_true",
                    help="after timing, rerun the workload in FP64 (untimed) and report the "
                         "origin-energy, total-energy and field errors of this precision")
     a = p.parse_args()
+    if a.steps is None:
+        a.steps = 300 if a.ensemble else 500
     if a.warmup < 0 or a.steps < 1:
         p.error("need --steps >= 1 and --warmup >= 0")
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     if a.impl == "reference":
         run_reference(a)
+    elif a.ensemble:
+        run_ensemble(a)
     else:
         run_gpu(a)
 

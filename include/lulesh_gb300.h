@@ -141,6 +141,51 @@ int lg_reset(lg_domain *d);
  * The FP64 leap-frog path is bound by this rate, not by HBM bandwidth. */
 int lg_measure_pipe(int op, int fp32, double *ginst_per_s);
 
+/* ---------------------------------------------------------------------------
+ * Ensembles: many independent problems advanced together.  No counterpart in
+ * the reference, which runs one problem per process; each member behaves as
+ * an lg_create problem with its own options (time step, stop test, cycle
+ * count, hourglass coefficient, deposited energy, regions), while every phase
+ * of the cycle is one launch over all members.
+ * ------------------------------------------------------------------------- */
+typedef struct lg_ensemble lg_ensemble;
+
+/* The ensemble study's problem set: nprob option sets drawn from seed with
+ * splitmix64 -- nx uniform in 16..64, einit_factor log-uniform in [0.5, 2],
+ * hgcoef uniform in [1, 3], numReg uniform in 4..16, balance 1, cost 1,
+ * its 300, precision LG_FP64, device 0. */
+int lg_ensemble_sample(int nprob, unsigned long long seed, lg_opts *out);
+
+/* Build nprob problems (opts[i] each; precision and device from opts[0]). */
+int lg_ensemble_create(int nprob, const lg_opts *opts, lg_ensemble **out);
+void lg_ensemble_destroy(lg_ensemble *en);
+
+/* Up to ncycles cycles of every member (each with its own loop test).
+ * Returns 0, or the status of the first member in error; per-member status
+ * through lg_ensemble_get_scalar(..., "status"). */
+int lg_ensemble_step(lg_ensemble *en, int ncycles);
+int lg_ensemble_step_timed(lg_ensemble *en, int ncycles, double *ms);
+
+/* Restore every member's set-up state. */
+int lg_ensemble_reset(lg_ensemble *en);
+
+/* Total elements and nodes over all members, and kernels queued so far. */
+int lg_ensemble_info(lg_ensemble *en, long long *total_elems, long long *total_nodes,
+                     long long *launches);
+
+/* Member prob's fields (double accessor fields; nodelist, regNumList, elemBC)
+ * and scalars (time deltatime dtcourant dthydro cycle status numElem numNode
+ * nx numReg hgcoef einit_factor its). */
+int lg_ensemble_get_field(lg_ensemble *en, int prob, const char *name, void *dst, size_t n);
+int lg_ensemble_get_scalar(lg_ensemble *en, int prob, const char *name, double *value);
+
+/* Times every block size (64, 128, 256) and grid shape (one pass over the
+ * members with resident blocks, or one thread per item) of each kernel for
+ * ncycles cycles on this ensemble, keeps the fastest, and restores the
+ * set-up state.  block_sizes[4] / persistent[4] receive the choice (either
+ * may be NULL). */
+int lg_ensemble_autotune(lg_ensemble *en, int ncycles, int *block_sizes, int *persistent);
+
 /* Nodal forces with no device allocation, for callers that own all device
  * memory themselves.  No counterpart in the reference: it exists for codes
  * that cannot let a library allocate behind their back -- hydro codes that

@@ -23,7 +23,7 @@ import os
 import numpy as np
 
 __all__ = ["Domain", "LuleshError", "VolumeError", "QStopError", "library_path", "load",
-           "FP64", "FP64_FMA", "MIXED", "NODE_FIELDS", "ELEM_FIELDS", "measure_pipe"]
+           "FP64", "FP64_FMA", "MIXED", "NODE_FIELDS", "ELEM_FIELDS", "measure_pipe", "Ensemble", "sample_ensemble"]
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_PKG, "lib", "liblulesh_gb300.so")
@@ -95,6 +95,19 @@ def load() -> ctypes.CDLL:
     lib.lg_profile.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_int)]
     lib.lg_reset.argtypes = [H]
+    lib.lg_ensemble_sample.argtypes = [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(_Opts)]
+    lib.lg_ensemble_create.argtypes = [ctypes.c_int, ctypes.POINTER(_Opts), ctypes.POINTER(H)]
+    lib.lg_ensemble_destroy.argtypes = [H]
+    lib.lg_ensemble_step.argtypes = [H, ctypes.c_int]
+    lib.lg_ensemble_step_timed.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.lg_ensemble_reset.argtypes = [H]
+    lib.lg_ensemble_info.argtypes = [H] + [ctypes.POINTER(ctypes.c_longlong)] * 3
+    lib.lg_ensemble_get_field.argtypes = [H, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p,
+                                          ctypes.c_size_t]
+    lib.lg_ensemble_get_scalar.argtypes = [H, ctypes.c_int, ctypes.c_char_p,
+                                           ctypes.POINTER(ctypes.c_double)]
+    lib.lg_ensemble_autotune.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_int)]
     lib.lg_measure_pipe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     lib.lg_last_error.restype = ctypes.c_char_p
     _lib = lib
@@ -284,3 +297,104 @@ class Domain:
         if st:
             _raise(st, self._lib)
         return buf.value.decode()
+
+
+_OPT_KEYS = ("nx", "numReg", "balance", "cost", "its", "hgcoef", "einit_factor")
+
+
+def sample_ensemble(nprob: int = 64, seed: int = 0) -> list[dict]:
+    """The ensemble study's problem set (lg_ensemble_sample): nx in 16..64,
+    log-uniform energy factor in [0.5, 2], hgcoef in [1, 3], 4..16 regions,
+    balance 1, cost 1, 300 cycles."""
+    lib = load()
+    arr = (_Opts * nprob)()
+    st = lib.lg_ensemble_sample(nprob, seed, arr)
+    if st:
+        _raise(st, lib)
+    return [{k: getattr(o, k) for k in _OPT_KEYS} for o in arr]
+
+
+class Ensemble:
+    """Many independent Sedov problems advanced together on one GPU
+    (lg_ensemble_*): each member keeps its own time step, cycle count and stop
+    test, while every phase of the cycle is one launch over all members."""
+
+    def __init__(self, members: list[dict], precision: str | int = "fp64", device: int = 0):
+        lib = load()
+        self._lib = lib
+        n = len(members)
+        arr = (_Opts * n)()
+        prec = _PRECISION[precision] if isinstance(precision, str) else int(precision)
+        for o, m in zip(arr, members):
+            lib.lg_default_opts(ctypes.byref(o))
+            for k, v in m.items():
+                setattr(o, k, v)
+            o.precision, o.device = prec, device
+        h = ctypes.c_void_p()
+        st = lib.lg_ensemble_create(n, arr, ctypes.byref(h))
+        if st:
+            _raise(st, lib)
+        self._h = h
+        self.members = [dict(m) for m in members]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lg_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, ncycles: int) -> int:
+        st = self._lib.lg_ensemble_step(self._h, int(ncycles))
+        if st > 0:
+            _raise(st, self._lib)
+        return st
+
+    def step_timed(self, ncycles: int) -> tuple[int, float]:
+        ms = ctypes.c_double()
+        st = self._lib.lg_ensemble_step_timed(self._h, int(ncycles), ctypes.byref(ms))
+        if st > 0:
+            _raise(st, self._lib)
+        return st, ms.value
+
+    def reset(self) -> None:
+        st = self._lib.lg_ensemble_reset(self._h)
+        if st:
+            _raise(st, self._lib)
+
+    def info(self) -> dict:
+        e, n, l = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        self._lib.lg_ensemble_info(self._h, ctypes.byref(e), ctypes.byref(n), ctypes.byref(l))
+        return {"elements": e.value, "nodes": n.value, "launches": l.value}
+
+    def autotune(self, ncycles: int = 3) -> dict:
+        bs = (ctypes.c_int * 4)()
+        pers = (ctypes.c_int * 4)()
+        st = self._lib.lg_ensemble_autotune(self._h, int(ncycles), bs, pers)
+        if st:
+            _raise(st, self._lib)
+        names = ("k_forces", "k_nodes", "k_kinematics", "k_material")
+        return {n: {"block": bs[i], "persistent": bool(pers[i])} for i, n in enumerate(names)}
+
+    def scalar(self, member: int, name: str) -> float:
+        v = ctypes.c_double()
+        st = self._lib.lg_ensemble_get_scalar(self._h, member, name.encode(), ctypes.byref(v))
+        if st:
+            _raise(st, self._lib)
+        return v.value
+
+    def field(self, member: int, name: str) -> np.ndarray:
+        nx = self.members[member]["nx"]
+        n = (nx + 1) ** 3 if name in NODE_FIELDS else nx ** 3
+        if name == "nodelist":
+            n = 8 * nx ** 3
+        dt = np.int32 if name in ("nodelist", "regNumList", "elemBC") else np.float64
+        out = np.empty(n, dtype=dt)
+        st = self._lib.lg_ensemble_get_field(self._h, member, name.encode(), out.ctypes.data, n)
+        if st:
+            _raise(st, self._lib)
+        return out

@@ -35,6 +35,7 @@ CUDA_UNITS = [
     ("lg_kernels_fma.cu", ["--fmad=true"]),
     ("lg_kernels_mixed.cu", ["--fmad=true"]),
     ("lg_api.cu", []),
+    ("lg_ensemble.cu", []),
     ("lg_peak.cu", ["--fmad=true"]),
     ("lg_noalloc.cu", ["--fmad=false"]),
 ]

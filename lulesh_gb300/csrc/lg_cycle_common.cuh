@@ -234,9 +234,10 @@ __device__ __forceinline__ double dmin_sel(double a, double b) { return (b < a) 
 // Reduces (dtc, dth) over the block; the last block of the grid reduces the
 // per-block results into ctl->dtcourant/dthydro, merges error flags and, if
 // advance, evaluates the loop condition and TimeIncrement of the next cycle.
-__device__ __forceinline__ void finish_dt(DevState &s, double dtc, double dth, bool advance)
+template <int BS>
+__device__ __forceinline__ void finish_dt(const DevState &s, double dtc, double dth, bool advance)
 {
-    __shared__ double red[2][kBlock / 32];
+    __shared__ double red[2][BS / 32];
     __shared__ bool am_last;
     Ctl *ctl = s.ctl;
 #pragma unroll
@@ -252,7 +253,7 @@ __device__ __forceinline__ void finish_dt(DevState &s, double dtc, double dth, b
     __syncthreads();
     if (threadIdx.x == 0) {
         double bc = red[0][0], bh = red[1][0];
-        for (int w = 1; w < kBlock / 32; ++w) {
+        for (int w = 1; w < BS / 32; ++w) {
             bc = dmin_sel(bc, red[0][w]);
             bh = dmin_sel(bh, red[1][w]);
         }
@@ -282,7 +283,7 @@ __device__ __forceinline__ void finish_dt(DevState &s, double dtc, double dth, b
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < kBlock / 32; ++w) {
+        for (int w = 1; w < BS / 32; ++w) {
             red[0][0] = dmin_sel(red[0][0], red[0][w]);
             red[1][0] = dmin_sel(red[1][0], red[1][w]);
         }
@@ -299,6 +300,111 @@ __device__ __forceinline__ void finish_dt(DevState &s, double dtc, double dth, b
         ctl->err_matvol = 0;
         if (advance) begin_cycle(ctl);
     }
+}
+
+
+// Merges the material phase's error flags once every block is done (the
+// qstop test precedes the material volume test, lulesh.cc:1993-2008, 2377).
+__device__ __forceinline__ void finish_material_flags(const DevState &s)
+{
+    __shared__ bool am_last;
+    Ctl *ctl = s.ctl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(&ctl->blocks_done, 1u);
+        am_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (am_last && threadIdx.x == 0) {
+        __threadfence();
+        ctl->blocks_done = 0;
+        if (ctl->status == 0) {
+            if (ctl->err_qstop)
+                ctl->status = -2;
+            else if (ctl->err_matvol)
+                ctl->status = -1;
+        }
+        ctl->err_qstop = 0;
+        ctl->err_matvol = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// batched problems: per-problem minima and the grid-wide end of the cycle
+// ---------------------------------------------------------------------------
+
+// Loop test + TimeIncrement of every problem (start of an ensemble step).
+__global__ void k_begin_all(Ctl *c, int n)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) begin_cycle(c + p);
+}
+
+// Folds this warp's Courant/hydro candidates into the per-problem slots.
+// Positive doubles order like their bit patterns, so an integer atomicMin is
+// an exact, order-independent minimum.  A warp inside one problem reduces
+// first and issues one atomic per slot.  pid < 0: no element.
+__device__ __forceinline__ void batched_dt_candidates(const DevState &s, int pid, double dtc,
+                                                      double dth)
+{
+    const unsigned full = 0xffffffffu;
+    unsigned long long c = (unsigned long long)__double_as_longlong(dtc);
+    unsigned long long h = (unsigned long long)__double_as_longlong(dth);
+    const unsigned long long big = (unsigned long long)__double_as_longlong(1.0e+20);
+    const int pid0 = __shfl_sync(full, pid, 0);
+    if (__all_sync(full, pid == pid0)) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const unsigned long long oc = __shfl_down_sync(full, c, off);
+            const unsigned long long oh = __shfl_down_sync(full, h, off);
+            c = oc < c ? oc : c;
+            h = oh < h ? oh : h;
+        }
+        if ((threadIdx.x & 31) == 0 && pid0 >= 0) {
+            if (c < big) atomicMin(&s.dtSlots[2 * pid0], c);
+            if (h < big) atomicMin(&s.dtSlots[2 * pid0 + 1], h);
+        }
+    } else if (pid >= 0) {
+        if (c < big) atomicMin(&s.dtSlots[2 * pid], c);
+        if (h < big) atomicMin(&s.dtSlots[2 * pid + 1], h);
+    }
+}
+
+// After every block of the batched material kernel: the last block takes each
+// live problem's minima (resetting the slots), merges its error flags and runs
+// its loop test and TimeIncrement for the next cycle.
+__device__ __forceinline__ void finish_batched(const DevState &s)
+{
+    __shared__ bool am_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(s.gridCounter, 1u);
+        am_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!am_last) return;
+    __threadfence();
+    const unsigned long long big = (unsigned long long)__double_as_longlong(1.0e+20);
+    for (int p = threadIdx.x; p < s.nprob; p += blockDim.x) {
+        Ctl *c = s.ctl + p;
+        if (!c->active) continue;
+        c->dtcourant = __longlong_as_double((long long)atomicExch(&s.dtSlots[2 * p], big));
+        c->dthydro = __longlong_as_double((long long)atomicExch(&s.dtSlots[2 * p + 1], big));
+        volatile int *vq = &c->err_qstop, *vm = &c->err_matvol;
+        if (c->status == 0) {
+            if (*vq)
+                c->status = -2;
+            else if (*vm)
+                c->status = -1;
+        }
+        *vq = 0;
+        *vm = 0;
+        begin_cycle(c);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *s.gridCounter = 0;
 }
 
 }  // namespace LG_NS

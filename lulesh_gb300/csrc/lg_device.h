@@ -68,8 +68,16 @@ struct DevState {
     // per-block minima of the time-constraint reduction
     double *dt_partial;
     int dt_blocks;
-    Ctl *ctl;
+    Ctl *ctl;  // nprob control blocks
     Params prm;
+    // batched problems (nprob > 1): owner of every element and node, each
+    // problem's hourglass coefficient, its Courant/hydro minimum slots (bit
+    // patterns of positive doubles) and the grid-wide block counter
+    int nprob;
+    uint16_t *elemProb, *nodeProb;
+    double *hgcoefs;
+    unsigned long long *dtSlots;
+    unsigned int *gridCounter;
 };
 
 }  // namespace lg

@@ -46,13 +46,11 @@ using namespace ::lg::geom;
 // ---------------------------------------------------------------------------
 // k_forces: CalcVolumeForceForElems (lulesh.cc:1062-1100)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_forces(DevState s)
+// one element; hourg is the element's problem's hourglass coefficient
+__device__ __forceinline__ void forces_element(const DevState &s, const int k, Ctl *ctl,
+                                               const double hourg)
 {
-    Ctl *ctl = s.ctl;
-    if (!cycle_live(ctl)) return;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int E = s.E;
-    if (k >= E) return;
     const size_t E8 = 8 * (size_t)E;
     double *const cs = s.corner;
 
@@ -86,7 +84,6 @@ __global__ void __launch_bounds__(kBlock) k_forces(DevState s)
     const double vk = s.v[k];
     const double determ = s.volo[k] * vk;
     if (vk <= 0.0) raise_status(ctl, -1);  // lulesh.cc:1034-1040
-    const double hourg = s.prm.hgcoef;
     if (!(hourg > 0.)) return;
 
     // CalcFBHourglassForceForElems (710-991), CalcElemFBHourglassForce (667-706)
@@ -137,24 +134,32 @@ __global__ void __launch_bounds__(kBlock) k_forces(DevState s)
     }
 }
 
+template <bool BATCHED, int BS>
+__global__ void __launch_bounds__(BS) k_forces(DevState s)
+{
+    if (!BATCHED && !cycle_live(s.ctl)) return;
+    for (int k = blockIdx.x * BS + threadIdx.x; k < s.E; k += gridDim.x * BS) {
+        const int pid = BATCHED ? s.elemProb[k] : 0;
+        Ctl *ctl = s.ctl + pid;
+        if (BATCHED && !cycle_live(ctl)) continue;
+        forces_element(s, k, ctl, BATCHED ? s.hgcoefs[pid] : s.prm.hgcoef);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // k_nodes: corner gather (lulesh.cc:565-582, 969-986), CalcAccelerationForNodes
 // (1139-1149), ApplyAccelerationBoundaryConditionsForNodes (1153-1179),
 // CalcVelocityForNodes (1183-1205), CalcPositionForNodes (1209-1219)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_nodes(DevState s)
+__device__ __forceinline__ void nodes_node(const DevState &s, const int n, const Ctl *ctl,
+                                           const bool hg)
 {
-    Ctl *ctl = s.ctl;
-    if (!cycle_live(ctl)) return;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= s.N) return;
     const int E = s.E;
     const size_t E8 = 8 * (size_t)E;
     const double *cs = s.corner;
     const int b = s.nodeElemStart[n], e = s.nodeElemStart[n + 1];
     double fx = 0.0, fy = 0.0, fz = 0.0;
     double hx = 0.0, hy = 0.0, hz = 0.0;
-    const bool hg = s.prm.hgcoef > 0.;
     for (int i = b; i < e; ++i) {
         const int c = s.nodeElemCornerList[i];
         const size_t idx = (size_t)(c & 7) * E + (c >> 3);
@@ -200,18 +205,26 @@ __global__ void __launch_bounds__(kBlock) k_nodes(DevState s)
     s.z[n] += zd * dt;
 }
 
+template <bool BATCHED, int BS>
+__global__ void __launch_bounds__(BS) k_nodes(DevState s)
+{
+    if (!BATCHED && !cycle_live(s.ctl)) return;
+    for (int n = blockIdx.x * BS + threadIdx.x; n < s.N; n += gridDim.x * BS) {
+        const int pid = BATCHED ? s.nodeProb[n] : 0;
+        const Ctl *ctl = s.ctl + pid;
+        if (BATCHED && !cycle_live(ctl)) continue;
+        nodes_node(s, n, ctl, (BATCHED ? s.hgcoefs[pid] : s.prm.hgcoef) > 0.);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // k_kinematics: CalcKinematicsForElems (lulesh.cc:1504-1568), the strain loop
 // of CalcLagrangeElements (1584-1606) and CalcMonotonicQGradientsForElems
 // (1613-1757)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_kinematics(DevState s)
+__device__ __forceinline__ void kinematics_element(const DevState &s, const int k, Ctl *ctl)
 {
-    Ctl *ctl = s.ctl;
-    if (!cycle_live(ctl)) return;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int E = s.E;
-    if (k >= E) return;
     int nd[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) nd[j] = __ldg(&s.nodelistT[(size_t)j * E + k]);
@@ -307,127 +320,140 @@ __global__ void __launch_bounds__(kBlock) k_kinematics(DevState s)
 #undef S4
 }
 
+template <bool BATCHED, int BS>
+__global__ void __launch_bounds__(BS) k_kinematics(DevState s)
+{
+    if (!BATCHED && !cycle_live(s.ctl)) return;
+    for (int k = blockIdx.x * BS + threadIdx.x; k < s.E; k += gridDim.x * BS) {
+        Ctl *ctl = s.ctl + (BATCHED ? s.elemProb[k] : 0);
+        if (BATCHED && !cycle_live(ctl)) continue;
+        kinematics_element(s, k, ctl);
+    }
+}
+
+// One element at region-order position t: monotonic-Q limiter, qstop check,
+// material update (MODE != 1) and its Courant/hydro candidates (MODE != 0).
+template <int MODE>
+__device__ __forceinline__ void material_element(const DevState &s, const int t, Ctl *ctl,
+                                                 double &dtc, double &dth)
+{
+    const Params &P = s.prm;
+    const int ielem = s.regPerm[t];
+    if (MODE != 1) {
+        // CalcMonotonicQRegionForElems, lulesh.cc:1761-1921
+        const int bc = s.elemBC[ielem];
+        const double phixi = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_xi, ielem, bc, XI_M_SYMM, XI_M_FREE,
+                                       XI_M, XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
+                                       s.lxip[ielem]);
+        const double phieta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_eta, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
+                                        ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P,
+                                        s.letam[ielem], s.letap[ielem]);
+        const double phizeta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_zeta, ielem, bc, ZETA_M_SYMM,
+                                         ZETA_M_FREE, ZETA_M, ZETA_P_SYMM, ZETA_P_FREE,
+                                         ZETA_P, s.lzetam[ielem], s.lzetap[ielem]);
+        const double vnew = s.vnew[ielem];
+        const double vdov = s.vdov[ielem];
+        double qlin, qquad;
+        if (vdov > 0.) {
+            qlin = 0.;
+            qquad = 0.;
+        } else {
+            double delvxxi = s.delv_xi[ielem] * s.delx_xi[ielem];
+            double delvxeta = s.delv_eta[ielem] * s.delx_eta[ielem];
+            double delvxzeta = s.delv_zeta[ielem] * s.delx_zeta[ielem];
+            if (delvxxi > 0.) delvxxi = 0.;
+            if (delvxeta > 0.) delvxeta = 0.;
+            if (delvxzeta > 0.) delvxzeta = 0.;
+            const double rho = s.elemMass[ielem] / (s.volo[ielem] * vnew);
+            qlin = -P.qlc_monoq * rho *
+                   (delvxxi * (1. - phixi) + delvxeta * (1. - phieta) +
+                    delvxzeta * (1. - phizeta));
+            qquad = P.qqc_monoq * rho *
+                    (delvxxi * delvxxi * (1. - phixi * phixi) +
+                     delvxeta * delvxeta * (1. - phieta * phieta) +
+                     delvxzeta * delvxzeta * (1. - phizeta * phizeta));
+        }
+        s.qq[ielem] = qquad;
+        s.ql[ielem] = qlin;
+
+        // qstop check on the previous cycle's q, lulesh.cc:1993-2008
+        const double q_old = s.q[ielem];
+        if (q_old > P.qstop) ctl->err_qstop = 1;
+
+        // ApplyMaterialPropertiesForElems, lulesh.cc:2328-2406
+        double vnewc = vnew;
+        if (P.eosvmin != 0. && vnewc < P.eosvmin) vnewc = P.eosvmin;
+        if (P.eosvmax != 0. && vnewc > P.eosvmax) vnewc = P.eosvmax;
+        double vc = s.v[ielem];
+        if (P.eosvmin != 0. && vc < P.eosvmin) vc = P.eosvmin;
+        if (P.eosvmax != 0. && vc > P.eosvmax) vc = P.eosvmax;
+        if (vc <= 0.) ctl->err_matvol = 1;
+
+        double p_new, e_new, q_new, ss_new;
+        eval_eos(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin, vnewc,
+                 s.regRep[t], p_new, e_new, q_new, ss_new);
+        s.p[ielem] = p_new;
+        s.e[ielem] = e_new;
+        s.q[ielem] = q_new;
+        s.ss[ielem] = ss_new;
+
+        // UpdateVolumesForElems, lulesh.cc:2410-2427
+        double tmpV = vnew;
+        if (fabs(tmpV - 1.0) < P.v_cut) tmpV = 1.0;
+        s.v[ielem] = tmpV;
+    }
+    if (MODE != 0) {
+        // CalcCourantConstraintForElems (2447-2513) and
+        // CalcHydroConstraintForElems (2517-2572) for one element
+        const double qqc2 = 64.0 * P.qqc * P.qqc;
+        const double ssv = s.ss[ielem];
+        const double vdov = s.vdov[ielem];
+        const double arealg = s.arealg[ielem];
+        double dtf = ssv * ssv;
+        if (vdov < 0.) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
+        dtf = sqrt(dtf);
+        dtf = arealg / dtf;
+        if (vdov != 0.) {
+            if (dtf < dtc) dtc = dtf;
+            const double dtdvov = P.dvovmax / (fabs(vdov) + 1.e-20);
+            if (dth > dtdvov) dth = dtdvov;
+        }
+    }
+}
+
 // MODE 0: Q limiter + qstop + EOS + sound speed + volume update (the part of
 //         LagrangeElements after the kinematics)
 // MODE 1: time constraints only (CalcTimeConstraintsForElems)
 // MODE 2: both, then the next cycle's TimeIncrement (the fused main loop)
-template <int MODE>
-__global__ void __launch_bounds__(kBlock) k_material(DevState s)
+// BATCHED (MODE 2 only): positions of many problems; each problem's minima go
+// to its slots, and the last block finishes every live problem's cycle.
+template <int MODE, bool BATCHED, int BS>
+__global__ void __launch_bounds__(BS) k_material(DevState s)
 {
-    Ctl *ctl = s.ctl;
-    if (!cycle_live(ctl)) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = t < s.E;
-    const Params &P = s.prm;
+    if (!BATCHED && !cycle_live(s.ctl)) return;
     double dtc = 1.0e+20, dth = 1.0e+20;
-    if (valid) {
-        const int ielem = s.regPerm[t];
-        if (MODE != 1) {
-            // CalcMonotonicQRegionForElems, lulesh.cc:1761-1921
-            const int bc = s.elemBC[ielem];
-            const double phixi = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_xi, ielem, bc, XI_M_SYMM, XI_M_FREE,
-                                           XI_M, XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
-                                           s.lxip[ielem]);
-            const double phieta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_eta, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
-                                            ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P,
-                                            s.letam[ielem], s.letap[ielem]);
-            const double phizeta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_zeta, ielem, bc, ZETA_M_SYMM,
-                                             ZETA_M_FREE, ZETA_M, ZETA_P_SYMM, ZETA_P_FREE,
-                                             ZETA_P, s.lzetam[ielem], s.lzetap[ielem]);
-            const double vnew = s.vnew[ielem];
-            const double vdov = s.vdov[ielem];
-            double qlin, qquad;
-            if (vdov > 0.) {
-                qlin = 0.;
-                qquad = 0.;
-            } else {
-                double delvxxi = s.delv_xi[ielem] * s.delx_xi[ielem];
-                double delvxeta = s.delv_eta[ielem] * s.delx_eta[ielem];
-                double delvxzeta = s.delv_zeta[ielem] * s.delx_zeta[ielem];
-                if (delvxxi > 0.) delvxxi = 0.;
-                if (delvxeta > 0.) delvxeta = 0.;
-                if (delvxzeta > 0.) delvxzeta = 0.;
-                const double rho = s.elemMass[ielem] / (s.volo[ielem] * vnew);
-                qlin = -P.qlc_monoq * rho *
-                       (delvxxi * (1. - phixi) + delvxeta * (1. - phieta) +
-                        delvxzeta * (1. - phizeta));
-                qquad = P.qqc_monoq * rho *
-                        (delvxxi * delvxxi * (1. - phixi * phixi) +
-                         delvxeta * delvxeta * (1. - phieta * phieta) +
-                         delvxzeta * delvxzeta * (1. - phizeta * phizeta));
-            }
-            s.qq[ielem] = qquad;
-            s.ql[ielem] = qlin;
-
-            // qstop check on the previous cycle's q, lulesh.cc:1993-2008
-            const double q_old = s.q[ielem];
-            if (q_old > P.qstop) ctl->err_qstop = 1;
-
-            // ApplyMaterialPropertiesForElems, lulesh.cc:2328-2406
-            double vnewc = vnew;
-            if (P.eosvmin != 0. && vnewc < P.eosvmin) vnewc = P.eosvmin;
-            if (P.eosvmax != 0. && vnewc > P.eosvmax) vnewc = P.eosvmax;
-            double vc = s.v[ielem];
-            if (P.eosvmin != 0. && vc < P.eosvmin) vc = P.eosvmin;
-            if (P.eosvmax != 0. && vc > P.eosvmax) vc = P.eosvmax;
-            if (vc <= 0.) ctl->err_matvol = 1;
-
-            double p_new, e_new, q_new, ss_new;
-            eval_eos(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin, vnewc,
-                     s.regRep[t], p_new, e_new, q_new, ss_new);
-            s.p[ielem] = p_new;
-            s.e[ielem] = e_new;
-            s.q[ielem] = q_new;
-            s.ss[ielem] = ss_new;
-
-            // UpdateVolumesForElems, lulesh.cc:2410-2427
-            double tmpV = vnew;
-            if (fabs(tmpV - 1.0) < P.v_cut) tmpV = 1.0;
-            s.v[ielem] = tmpV;
-        }
-        if (MODE != 0) {
-            // CalcCourantConstraintForElems (2447-2513) and
-            // CalcHydroConstraintForElems (2517-2572) for one element
-            const double qqc2 = 64.0 * P.qqc * P.qqc;
-            const double ssv = s.ss[ielem];
-            const double vdov = s.vdov[ielem];
-            const double arealg = s.arealg[ielem];
-            double dtf = ssv * ssv;
-            if (vdov < 0.) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
-            dtf = sqrt(dtf);
-            dtf = arealg / dtf;
-            if (vdov != 0.) {
-                if (dtf < dtc) dtc = dtf;
-                const double dtdvov = P.dvovmax / (fabs(vdov) + 1.e-20);
-                if (dth > dtdvov) dth = dtdvov;
-            }
-        }
+    if (!BATCHED) {
+        const int t = blockIdx.x * BS + threadIdx.x;
+        if (t < s.E) material_element<MODE>(s, t, s.ctl, dtc, dth);
+        if (MODE != 0)
+            finish_dt<BS>(s, dtc, dth, MODE == 2);
+        else
+            finish_material_flags(s);
+        return;
     }
-    if (MODE != 0) {
-        finish_dt(s, dtc, dth, MODE == 2);
-    } else {
-        // merge the material-phase error flags once every block is done
-        __shared__ bool am_last;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            const unsigned prev = atomicAdd(&ctl->blocks_done, 1u);
-            am_last = (prev == gridDim.x - 1);
+    for (int t0 = blockIdx.x * BS; t0 < s.E; t0 += gridDim.x * BS) {
+        const int t = t0 + threadIdx.x;
+        int pid = -1;
+        dtc = 1.0e+20;
+        dth = 1.0e+20;
+        if (t < s.E) {
+            pid = s.elemProb[s.regPerm[t]];
+            Ctl *ctl = s.ctl + pid;
+            if (cycle_live(ctl)) material_element<2>(s, t, ctl, dtc, dth);
         }
-        __syncthreads();
-        if (am_last && threadIdx.x == 0) {
-            __threadfence();
-            ctl->blocks_done = 0;
-            if (ctl->status == 0) {
-                if (ctl->err_qstop)
-                    ctl->status = -2;
-                else if (ctl->err_matvol)
-                    ctl->status = -1;
-            }
-            ctl->err_qstop = 0;
-            ctl->err_matvol = 0;
-        }
+        batched_dt_candidates(s, pid, dtc, dth);
     }
+    finish_batched(s);
 }
 
 }  // namespace LG_NS

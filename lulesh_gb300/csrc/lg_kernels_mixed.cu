@@ -42,13 +42,10 @@ __device__ __forceinline__ void relative_coords(const DevState &s, const int nd[
 }
 
 // CalcVolumeForceForElems (lulesh.cc:1062-1100) in FP32
-__global__ void __launch_bounds__(kBlock) k_forces(DevState s)
+__device__ __forceinline__ void forces_element(const DevState &s, const int k, Ctl *ctl,
+                                               const double hg64)
 {
-    Ctl *ctl = s.ctl;
-    if (!cycle_live(ctl)) return;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int E = s.E;
-    if (k >= E) return;
     const size_t E8 = 8 * (size_t)E;
     float *const cs = fview(s.corner);
     int nd[8];
@@ -71,7 +68,6 @@ __global__ void __launch_bounds__(kBlock) k_forces(DevState s)
     }
     const double vk = s.v[k];
     if (vk <= 0.0) raise_status(ctl, -1);
-    const double hg64 = s.prm.hgcoef;
     if (!(hg64 > 0.)) return;
     const float determ = to_f32(s.volo[k]) * to_f32(vk);
     float hourgam[8][4];
@@ -118,20 +114,28 @@ __global__ void __launch_bounds__(kBlock) k_forces(DevState s)
     }
 }
 
+template <bool BATCHED, int BS>
+__global__ void __launch_bounds__(BS) k_forces(DevState s)
+{
+    if (!BATCHED && !cycle_live(s.ctl)) return;
+    for (int k = blockIdx.x * BS + threadIdx.x; k < s.E; k += gridDim.x * BS) {
+        const int pid = BATCHED ? s.elemProb[k] : 0;
+        Ctl *ctl = s.ctl + pid;
+        if (BATCHED && !cycle_live(ctl)) continue;
+        forces_element(s, k, ctl, BATCHED ? s.hgcoefs[pid] : s.prm.hgcoef);
+    }
+}
+
 // ordered FP32 corner gather, then LagrangeNodal's FP64 node update
 // (lulesh.cc:1139-1219)
-__global__ void __launch_bounds__(kBlock) k_nodes(DevState s)
+__device__ __forceinline__ void nodes_node(const DevState &s, const int n, const Ctl *ctl,
+                                           const bool hg)
 {
-    Ctl *ctl = s.ctl;
-    if (!cycle_live(ctl)) return;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= s.N) return;
     const int E = s.E;
     const size_t E8 = 8 * (size_t)E;
     const float *cs = fview(s.corner);
     const int b = s.nodeElemStart[n], e = s.nodeElemStart[n + 1];
     float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
-    const bool hg = s.prm.hgcoef > 0.;
     for (int i = b; i < e; ++i) {
         const int c = s.nodeElemCornerList[i];
         const size_t idx = (size_t)(c & 7) * E + (c >> 3);
@@ -178,15 +182,23 @@ __global__ void __launch_bounds__(kBlock) k_nodes(DevState s)
     s.z[n] += zd * dt;
 }
 
+template <bool BATCHED, int BS>
+__global__ void __launch_bounds__(BS) k_nodes(DevState s)
+{
+    if (!BATCHED && !cycle_live(s.ctl)) return;
+    for (int n = blockIdx.x * BS + threadIdx.x; n < s.N; n += gridDim.x * BS) {
+        const int pid = BATCHED ? s.nodeProb[n] : 0;
+        const Ctl *ctl = s.ctl + pid;
+        if (BATCHED && !cycle_live(ctl)) continue;
+        nodes_node(s, n, ctl, (BATCHED ? s.hgcoefs[pid] : s.prm.hgcoef) > 0.);
+    }
+}
+
 // CalcKinematicsForElems + CalcMonotonicQGradientsForElems
 // (lulesh.cc:1504-1757): FP64 volume, FP32 the rest
-__global__ void __launch_bounds__(kBlock) k_kinematics(DevState s)
+__device__ __forceinline__ void kinematics_element(const DevState &s, const int k, Ctl *ctl)
 {
-    Ctl *ctl = s.ctl;
-    if (!cycle_live(ctl)) return;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int E = s.E;
-    if (k >= E) return;
     int nd[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) nd[j] = __ldg(&s.nodelistT[(size_t)j * E + k]);
@@ -297,121 +309,131 @@ __global__ void __launch_bounds__(kBlock) k_kinematics(DevState s)
 #undef S4
 }
 
-// Q limiter (FP32) + material update (FP64 EOS) + time constraints (FP64);
-// MODE as in the FP64 kernels
-template <int MODE>
-__global__ void __launch_bounds__(kBlock) k_material(DevState s)
+template <bool BATCHED, int BS>
+__global__ void __launch_bounds__(BS) k_kinematics(DevState s)
 {
-    Ctl *ctl = s.ctl;
-    if (!cycle_live(ctl)) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = t < s.E;
+    if (!BATCHED && !cycle_live(s.ctl)) return;
+    for (int k = blockIdx.x * BS + threadIdx.x; k < s.E; k += gridDim.x * BS) {
+        Ctl *ctl = s.ctl + (BATCHED ? s.elemProb[k] : 0);
+        if (BATCHED && !cycle_live(ctl)) continue;
+        kinematics_element(s, k, ctl);
+    }
+}
+
+// Q limiter (FP32) + material update (FP64 EOS) + time constraints (FP64)
+// for one element at region-order position t; MODE as in the FP64 kernels
+template <int MODE>
+__device__ __forceinline__ void material_element(const DevState &s, const int t, Ctl *ctl,
+                                                 double &dtc, double &dth)
+{
     const Params &P = s.prm;
-    double dtc = 1.0e+20, dth = 1.0e+20;
-    if (valid) {
-        const int ielem = s.regPerm[t];
-        if (MODE != 1) {
-            const float lm = to_f32(P.monoq_limiter_mult), ms = to_f32(P.monoq_max_slope);
-            const float *gvx = fview(s.delv_xi), *gve = fview(s.delv_eta),
-                        *gvz = fview(s.delv_zeta);
-            const int bc = s.elemBC[ielem];
-            const float phixi = monoq_phi(lm, ms, gvx, ielem, bc, XI_M_SYMM, XI_M_FREE, XI_M,
-                                          XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
-                                          s.lxip[ielem]);
-            const float phieta = monoq_phi(lm, ms, gve, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
-                                           ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P, s.letam[ielem],
-                                           s.letap[ielem]);
-            const float phizeta = monoq_phi(lm, ms, gvz, ielem, bc, ZETA_M_SYMM, ZETA_M_FREE,
-                                            ZETA_M, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P,
-                                            s.lzetam[ielem], s.lzetap[ielem]);
-            const double vnew = s.vnew[ielem];
-            const double vdov = s.vdov[ielem];
-            double qlin, qquad;
-            if (FastOps::lt(0.0, vdov)) {
-                qlin = 0.;
-                qquad = 0.;
-            } else {
-                float dxxi = gvx[ielem] * fview(s.delx_xi)[ielem];
-                float dxeta = gve[ielem] * fview(s.delx_eta)[ielem];
-                float dxzeta = gvz[ielem] * fview(s.delx_zeta)[ielem];
-                if (dxxi > 0.f) dxxi = 0.f;
-                if (dxeta > 0.f) dxeta = 0.f;
-                if (dxzeta > 0.f) dxzeta = 0.f;
-                const float rho = to_f32(s.elemMass[ielem]) /
-                                  (to_f32(s.volo[ielem]) * to_f32(vnew));
-                qlin = to_f64(-to_f32(P.qlc_monoq) * rho *
-                              (dxxi * (1.f - phixi) + dxeta * (1.f - phieta) +
-                               dxzeta * (1.f - phizeta)));
-                qquad = to_f64(to_f32(P.qqc_monoq) * rho *
-                               (dxxi * dxxi * (1.f - phixi * phixi) +
-                                dxeta * dxeta * (1.f - phieta * phieta) +
-                                dxzeta * dxzeta * (1.f - phizeta * phizeta)));
-            }
-            s.qq[ielem] = qquad;
-            s.ql[ielem] = qlin;
-
-            const double q_old = s.q[ielem];
-            if (FastOps::lt(P.qstop, q_old)) ctl->err_qstop = 1;
-
-            double vnewc = vnew;
-            if (P.eosvmin != 0. && FastOps::lt(vnewc, P.eosvmin)) vnewc = P.eosvmin;
-            if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vnewc)) vnewc = P.eosvmax;
-            double vc = s.v[ielem];
-            if (P.eosvmin != 0. && FastOps::lt(vc, P.eosvmin)) vc = P.eosvmin;
-            if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vc)) vc = P.eosvmax;
-            if (FastOps::le(vc, 0.)) ctl->err_matvol = 1;
-
-            double p_new, e_new, q_new, ss_new;
-            eval_eos<FastOps>(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin,
-                              vnewc, s.regRep[t], p_new, e_new, q_new, ss_new);
-            s.p[ielem] = p_new;
-            s.e[ielem] = e_new;
-            s.q[ielem] = q_new;
-            s.ss[ielem] = ss_new;
-
-            double tmpV = vnew;
-            if (FastOps::abs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
-            s.v[ielem] = tmpV;
+    const int ielem = s.regPerm[t];
+    if (MODE != 1) {
+        const float lm = to_f32(P.monoq_limiter_mult), ms = to_f32(P.monoq_max_slope);
+        const float *gvx = fview(s.delv_xi), *gve = fview(s.delv_eta),
+                    *gvz = fview(s.delv_zeta);
+        const int bc = s.elemBC[ielem];
+        const float phixi = monoq_phi(lm, ms, gvx, ielem, bc, XI_M_SYMM, XI_M_FREE, XI_M,
+                                      XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
+                                      s.lxip[ielem]);
+        const float phieta = monoq_phi(lm, ms, gve, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
+                                       ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P, s.letam[ielem],
+                                       s.letap[ielem]);
+        const float phizeta = monoq_phi(lm, ms, gvz, ielem, bc, ZETA_M_SYMM, ZETA_M_FREE,
+                                        ZETA_M, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P,
+                                        s.lzetam[ielem], s.lzetap[ielem]);
+        const double vnew = s.vnew[ielem];
+        const double vdov = s.vdov[ielem];
+        double qlin, qquad;
+        if (FastOps::lt(0.0, vdov)) {
+            qlin = 0.;
+            qquad = 0.;
+        } else {
+            float dxxi = gvx[ielem] * fview(s.delx_xi)[ielem];
+            float dxeta = gve[ielem] * fview(s.delx_eta)[ielem];
+            float dxzeta = gvz[ielem] * fview(s.delx_zeta)[ielem];
+            if (dxxi > 0.f) dxxi = 0.f;
+            if (dxeta > 0.f) dxeta = 0.f;
+            if (dxzeta > 0.f) dxzeta = 0.f;
+            const float rho = to_f32(s.elemMass[ielem]) /
+                              (to_f32(s.volo[ielem]) * to_f32(vnew));
+            qlin = to_f64(-to_f32(P.qlc_monoq) * rho *
+                          (dxxi * (1.f - phixi) + dxeta * (1.f - phieta) +
+                           dxzeta * (1.f - phizeta)));
+            qquad = to_f64(to_f32(P.qqc_monoq) * rho *
+                           (dxxi * dxxi * (1.f - phixi * phixi) +
+                            dxeta * dxeta * (1.f - phieta * phieta) +
+                            dxzeta * dxzeta * (1.f - phizeta * phizeta)));
         }
-        if (MODE != 0) {
-            const double qqc2 = 64.0 * P.qqc * P.qqc;
-            const double ssv = s.ss[ielem];
-            const double vdov = s.vdov[ielem];
-            const double arealg = s.arealg[ielem];
-            double dtf = ssv * ssv;
-            if (FastOps::lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
-            dtf = arealg * rcp_nr(sqrt_nr(dtf));
-            if (vdov != 0.) {
-                if (dtf < dtc) dtc = dtf;
-                const double dtdvov = P.dvovmax * rcp_nr(fabs(vdov) + 1.e-20);
-                if (dth > dtdvov) dth = dtdvov;
-            }
-        }
+        s.qq[ielem] = qquad;
+        s.ql[ielem] = qlin;
+
+        const double q_old = s.q[ielem];
+        if (FastOps::lt(P.qstop, q_old)) ctl->err_qstop = 1;
+
+        double vnewc = vnew;
+        if (P.eosvmin != 0. && FastOps::lt(vnewc, P.eosvmin)) vnewc = P.eosvmin;
+        if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vnewc)) vnewc = P.eosvmax;
+        double vc = s.v[ielem];
+        if (P.eosvmin != 0. && FastOps::lt(vc, P.eosvmin)) vc = P.eosvmin;
+        if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vc)) vc = P.eosvmax;
+        if (FastOps::le(vc, 0.)) ctl->err_matvol = 1;
+
+        double p_new, e_new, q_new, ss_new;
+        eval_eos<FastOps>(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin,
+                          vnewc, s.regRep[t], p_new, e_new, q_new, ss_new);
+        s.p[ielem] = p_new;
+        s.e[ielem] = e_new;
+        s.q[ielem] = q_new;
+        s.ss[ielem] = ss_new;
+
+        double tmpV = vnew;
+        if (FastOps::abs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
+        s.v[ielem] = tmpV;
     }
     if (MODE != 0) {
-        finish_dt(s, dtc, dth, MODE == 2);
-    } else {
-        __shared__ bool am_last;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            const unsigned prev = atomicAdd(&ctl->blocks_done, 1u);
-            am_last = (prev == gridDim.x - 1);
-        }
-        __syncthreads();
-        if (am_last && threadIdx.x == 0) {
-            __threadfence();
-            ctl->blocks_done = 0;
-            if (ctl->status == 0) {
-                if (ctl->err_qstop)
-                    ctl->status = -2;
-                else if (ctl->err_matvol)
-                    ctl->status = -1;
-            }
-            ctl->err_qstop = 0;
-            ctl->err_matvol = 0;
+        const double qqc2 = 64.0 * P.qqc * P.qqc;
+        const double ssv = s.ss[ielem];
+        const double vdov = s.vdov[ielem];
+        const double arealg = s.arealg[ielem];
+        double dtf = ssv * ssv;
+        if (FastOps::lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
+        dtf = arealg * rcp_nr(sqrt_nr(dtf));
+        if (vdov != 0.) {
+            if (dtf < dtc) dtc = dtf;
+            const double dtdvov = P.dvovmax * rcp_nr(fabs(vdov) + 1.e-20);
+            if (dth > dtdvov) dth = dtdvov;
         }
     }
+}
+
+template <int MODE, bool BATCHED, int BS>
+__global__ void __launch_bounds__(BS) k_material(DevState s)
+{
+    if (!BATCHED && !cycle_live(s.ctl)) return;
+    double dtc = 1.0e+20, dth = 1.0e+20;
+    if (!BATCHED) {
+        const int t = blockIdx.x * BS + threadIdx.x;
+        if (t < s.E) material_element<MODE>(s, t, s.ctl, dtc, dth);
+        if (MODE != 0)
+            finish_dt<BS>(s, dtc, dth, MODE == 2);
+        else
+            finish_material_flags(s);
+        return;
+    }
+    for (int t0 = blockIdx.x * BS; t0 < s.E; t0 += gridDim.x * BS) {
+        const int t = t0 + threadIdx.x;
+        int pid = -1;
+        dtc = 1.0e+20;
+        dth = 1.0e+20;
+        if (t < s.E) {
+            pid = s.elemProb[s.regPerm[t]];
+            Ctl *ctl = s.ctl + pid;
+            if (cycle_live(ctl)) material_element<2>(s, t, ctl, dtc, dth);
+        }
+        batched_dt_candidates(s, pid, dtc, dth);
+    }
+    finish_batched(s);
 }
 
 }  // namespace mixed

@@ -20,6 +20,10 @@ struct KernelSet {
     void (*set_active)(Ctl *ctl, cudaStream_t st);
     // id < K_COUNT; mode selects the k_material variant (0, 1 or 2)
     void (*launch)(int id, const DevState &s, int mode, cudaStream_t st);
+    // batched problems (DevState::nprob > 1)
+    void (*launch_batched)(int id, const DevState &s, int bs, int grid, cudaStream_t st);
+    void (*begin_all)(Ctl *ctl, int nprob, cudaStream_t st);
+    int (*occupancy)(int id, int bs);
     const char *kernel_names[K_COUNT];
     int material_blocks(int E) const { return (E + 127) / 128; }
 };

@@ -1,0 +1,63 @@
+"""Batched ensemble: every member must evolve exactly as the same problem run
+alone through lg_create/lg_step (same arithmetic, same order), each with its
+own time step and stop test."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MEMBERS = [
+    {"nx": 6, "numReg": 4, "balance": 1, "cost": 1, "its": 40, "hgcoef": 1.4, "einit_factor": 0.6},
+    {"nx": 11, "numReg": 9, "balance": 1, "cost": 1, "its": 40, "hgcoef": 2.7, "einit_factor": 1.8},
+    {"nx": 4, "numReg": 5, "balance": 1, "cost": 2, "its": 100, "hgcoef": 3.0, "einit_factor": 1.0},
+    {"nx": 14, "numReg": 16, "balance": 2, "cost": 4, "its": 30, "hgcoef": 2.0, "einit_factor": 0.9},
+    {"nx": 9, "numReg": 11, "balance": 1, "cost": 1, "its": 40, "hgcoef": 1.0, "einit_factor": 1.3},
+]
+
+
+def _bits(a):
+    return a.view(np.int64)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_members_equal_single_problem_runs(native_lib, precision):
+    import lulesh_gb300 as lg
+    en = lg.Ensemble(MEMBERS, precision=precision)
+    assert en.step(100) == 0
+    for i, m in enumerate(MEMBERS):
+        d = lg.Domain(m["nx"], m["numReg"], m["balance"], m["cost"], its=m["its"],
+                      hgcoef=m["hgcoef"], einit_factor=m["einit_factor"], precision=precision)
+        assert d.run() == 0
+        assert en.scalar(i, "cycle") == d.cycle
+        assert en.scalar(i, "time") == d.time
+        for f in lg.NODE_FIELDS + lg.ELEM_FIELDS:
+            assert np.array_equal(_bits(en.field(i, f)), _bits(d.field(f))), (i, f)
+        d.close()
+    # the s=4 member reaches stoptime (45 cycles) before its 100-cycle limit
+    assert en.scalar(2, "cycle") == 45
+
+
+def test_autotune_keeps_results_and_reset(native_lib):
+    import lulesh_gb300 as lg
+    a = lg.Ensemble(MEMBERS)
+    assert a.step(20) == 0
+    ref = [a.field(i, "e").copy() for i in range(len(MEMBERS))]
+    b = lg.Ensemble(MEMBERS)
+    choice = b.autotune(2)
+    assert set(choice) == {"k_forces", "k_nodes", "k_kinematics", "k_material"}
+    assert all(c["block"] in (64, 128, 256) for c in choice.values())
+    assert b.scalar(0, "cycle") == 0  # the tuning cycles were undone
+    assert b.step(20) == 0
+    for i in range(len(MEMBERS)):
+        assert np.array_equal(_bits(b.field(i, "e")), _bits(ref[i])), i
+
+
+def test_sampled_ensemble_runs(native_lib):
+    import lulesh_gb300 as lg
+    members = lg.sample_ensemble(8, seed=0)
+    for m in members:
+        m["nx"] = min(m["nx"], 20)  # keep the test small
+        m["its"] = 10
+    en = lg.Ensemble(members)
+    assert en.step(10) == 0
+    assert all(en.scalar(i, "cycle") == 10 for i in range(8))

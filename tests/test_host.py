@@ -114,3 +114,16 @@ def test_cli_help_and_parse_errors(native_lib):
     assert r.returncode == 255 and "Missing integer argument to -i" in r.stdout
     r = subprocess.run([cli, "-x"], capture_output=True, text=True)
     assert r.returncode == 255 and "Unknown command line argument: -x" in r.stdout
+
+
+def test_ensemble_sample_is_deterministic_and_in_range(native_lib):
+    import lulesh_gb300 as lg
+    a = lg.sample_ensemble(64, seed=0)
+    b = lg.sample_ensemble(64, seed=0)
+    assert a == b
+    assert a != lg.sample_ensemble(64, seed=1)
+    for m in a:
+        assert 16 <= m["nx"] <= 64 and 4 <= m["numReg"] <= 16
+        assert 1.0 <= m["hgcoef"] <= 3.0 and 0.5 <= m["einit_factor"] <= 2.0
+        assert m["balance"] == 1 and m["cost"] == 1 and m["its"] == 300
+    assert len({m["nx"] for m in a}) > 20  # the sizes really vary
