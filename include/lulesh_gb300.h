@@ -142,6 +142,33 @@ int lg_reset(lg_domain *d);
 int lg_measure_pipe(int op, int fp32, double *ginst_per_s);
 
 /* ---------------------------------------------------------------------------
+ * Frozen time steps and the adjoint.  No counterpart in the reference, whose
+ * time step always comes from TimeIncrement (lulesh.cc:166-222).
+ * ------------------------------------------------------------------------- */
+
+/* Record the time step of every following cycle: cycle c (0-based count of
+ * completed cycles when it starts) stores its dt at index c < capacity.
+ * capacity 0 stops recording.  lg_dt_get copies the first n entries. */
+int lg_dt_record(lg_domain *d, int capacity);
+int lg_dt_get(lg_domain *d, double *out, int n);
+
+/* Freeze the time steps: cycle c uses dts[c] (c < n) instead of
+ * TimeIncrement's selection.  n = 0 unfreezes.  Survives lg_reset. */
+int lg_dt_freeze(lg_domain *d, const double *dts, int n);
+
+/* Reverse-mode gradient of J = sum over elements i with mask[i] != 0 of
+ * e_i * volo_i after ncycles cycles (the total internal energy of the
+ * masked elements), with respect to the energy field e of the current state
+ * (dJ_de0, numElem entries) and the hourglass coefficient (*dJ_dhgcoef).
+ * The time steps must be frozen for these cycles (lg_dt_freeze).  Runs the
+ * forward cycles with a checkpoint every ckpt_k cycles, recomputes each
+ * segment and sweeps it backwards; leaves the handle in the final state and
+ * returns *J.  Non-smooth operations (cut-offs, clamps, the monotonic
+ * limiter) contribute the derivative of the branch taken.  FP64 paths only. */
+int lg_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask, double *J,
+               double *dJ_de0, double *dJ_dhgcoef);
+
+/* ---------------------------------------------------------------------------
  * Ensembles: many independent problems advanced together.  No counterpart in
  * the reference, which runs one problem per process; each member behaves as
  * an lg_create problem with its own options (time step, stop test, cycle

@@ -95,6 +95,12 @@ def load() -> ctypes.CDLL:
     lib.lg_profile.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_int)]
     lib.lg_reset.argtypes = [H]
+    lib.lg_dt_record.argtypes = [H, ctypes.c_int]
+    lib.lg_dt_get.argtypes = [H, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    lib.lg_dt_freeze.argtypes = [H, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    lib.lg_adjoint.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_ubyte),
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double)]
     lib.lg_ensemble_sample.argtypes = [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(_Opts)]
     lib.lg_ensemble_create.argtypes = [ctypes.c_int, ctypes.POINTER(_Opts), ctypes.POINTER(H)]
     lib.lg_ensemble_destroy.argtypes = [H]
@@ -202,6 +208,47 @@ class Domain:
         st = self._lib.lg_reset(self._h)
         if st:
             _raise(st, self._lib)
+
+    # frozen time steps and the adjoint ------------------------------------
+    def dt_record(self, capacity: int) -> None:
+        """Record every following cycle's time step (index = cycle number)."""
+        st = self._lib.lg_dt_record(self._h, int(capacity))
+        if st:
+            _raise(st, self._lib)
+
+    def dt_get(self, n: int) -> np.ndarray:
+        out = np.empty(n, dtype=np.float64)
+        st = self._lib.lg_dt_get(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n)
+        if st:
+            _raise(st, self._lib)
+        return out
+
+    def dt_freeze(self, dts) -> None:
+        """Cycle c uses dts[c] instead of TimeIncrement (empty: unfreeze)."""
+        a = np.ascontiguousarray(dts, dtype=np.float64)
+        st = self._lib.lg_dt_freeze(self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                    a.size)
+        if st:
+            _raise(st, self._lib)
+
+    def adjoint(self, ncycles: int, mask, ckpt: int = 20) -> tuple[float, np.ndarray, float]:
+        """J = sum(e * volo over mask) after ncycles frozen-dt cycles from the
+        current state, and its gradients with respect to the current energy
+        field and hgcoef (lg_adjoint)."""
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        if m.size != self.numElem:
+            raise ValueError("mask needs one entry per element")
+        J = ctypes.c_double()
+        ge = np.empty(self.numElem, dtype=np.float64)
+        gh = ctypes.c_double()
+        st = self._lib.lg_adjoint(self._h, int(ncycles), int(ckpt),
+                                  m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)),
+                                  ctypes.byref(J),
+                                  ge.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  ctypes.byref(gh))
+        if st:
+            _raise(st, self._lib)
+        return J.value, ge, gh.value
 
     def phase(self, which: int) -> int:
         return self._status(self._lib.lg_phase(self._h, int(which)), False)

@@ -36,6 +36,7 @@ CUDA_UNITS = [
     ("lg_kernels_mixed.cu", ["--fmad=true"]),
     ("lg_api.cu", []),
     ("lg_ensemble.cu", []),
+    ("lg_adjoint.cu", ["--fmad=true"]),
     ("lg_peak.cu", ["--fmad=true"]),
     ("lg_noalloc.cu", ["--fmad=false"]),
 ]

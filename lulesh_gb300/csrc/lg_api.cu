@@ -73,7 +73,26 @@ struct lg_domain {
     int its = 9999999;
     bool host_only = false;  // device < 0: problem set-up only, no GPU
     long long launches = 0;  // kernels queued by this handle
+    // frozen / recorded time steps (lg_dt_freeze, lg_dt_record)
+    double *d_dtfrozen = nullptr, *d_dtrec = nullptr;
+    int dtfrozen_len = 0, dtrec_len = 0;
+    std::vector<double> h_dtfrozen;
 };
+
+namespace lg {
+struct AdjointIO {
+    const DevState *ds;
+    const KernelSet *ks;
+    cudaStream_t stream;
+    Ctl *h_ctl;
+    const double *dts;
+    int ncycles, ckpt_k;
+    const unsigned char *mask;
+    double hgcoef;
+    const std::vector<int> *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *elemBC;
+};
+int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg);
+}  // namespace lg
 
 namespace {
 
@@ -323,6 +342,10 @@ int upload_initial_state(lg_domain *d)
     c.dtmultub = p.t.deltatimemultub;
     c.cycle = p.t.cycle;
     c.cycle_limit = 0;
+    c.dt_frozen = d->d_dtfrozen;
+    c.dt_frozen_len = d->dtfrozen_len;
+    c.dt_record = d->d_dtrec;
+    c.dt_record_len = d->dtrec_len;
     return write_ctl(d);
 }
 
@@ -469,6 +492,8 @@ void lg_destroy(lg_domain *d)
     cudaSetDevice(d->opts.device);
     if (d->stream) cudaStreamSynchronize(d->stream);
     drop_graphs(d);
+    if (d->d_dtfrozen) cudaFree(d->d_dtfrozen);
+    if (d->d_dtrec) cudaFree(d->d_dtrec);
     if (d->ev0) cudaEventDestroy(d->ev0);
     if (d->ev1) cudaEventDestroy(d->ev1);
     if (d->h_ctl) cudaFreeHost(d->h_ctl);
@@ -779,6 +804,85 @@ int lg_report(lg_domain *d, double elapsed, char *buf, size_t buflen)
                                             elapsed);
     snprintf(buf, buflen, "%s", s.c_str());
     return LG_OK;
+}
+
+int lg_dt_record(lg_domain *d, int capacity)
+{
+    if (!d || capacity < 0) return set_error(LG_ERR_INVALID, "invalid argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    if (d->d_dtrec) cudaFree(d->d_dtrec);
+    d->d_dtrec = nullptr;
+    d->dtrec_len = 0;
+    if (capacity > 0) {
+        LG_CUDA(cudaMalloc(&d->d_dtrec, sizeof(double) * (size_t)capacity));
+        LG_CUDA(cudaMemsetAsync(d->d_dtrec, 0, sizeof(double) * (size_t)capacity, d->stream));
+        d->dtrec_len = capacity;
+    }
+    if ((st = read_ctl(d))) return st;
+    d->h_ctl->dt_record = d->d_dtrec;
+    d->h_ctl->dt_record_len = d->dtrec_len;
+    return write_ctl(d);
+}
+
+int lg_dt_get(lg_domain *d, double *out, int n)
+{
+    if (!d || !out || n < 0 || n > d->dtrec_len) return set_error(LG_ERR_INVALID, "invalid argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    if (n == 0) return LG_OK;
+    LG_CUDA(cudaMemcpyAsync(out, d->d_dtrec, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost,
+                            d->stream));
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    return LG_OK;
+}
+
+int lg_dt_freeze(lg_domain *d, const double *dts, int n)
+{
+    if (!d || n < 0 || (n > 0 && !dts)) return set_error(LG_ERR_INVALID, "invalid argument");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    if (d->d_dtfrozen) cudaFree(d->d_dtfrozen);
+    d->d_dtfrozen = nullptr;
+    d->dtfrozen_len = 0;
+    d->h_dtfrozen.assign(dts, dts + n);
+    if (n > 0) {
+        LG_CUDA(cudaMalloc(&d->d_dtfrozen, sizeof(double) * (size_t)n));
+        LG_CUDA(cudaMemcpyAsync(d->d_dtfrozen, dts, sizeof(double) * (size_t)n,
+                                cudaMemcpyHostToDevice, d->stream));
+        d->dtfrozen_len = n;
+    }
+    if ((st = read_ctl(d))) return st;
+    d->h_ctl->dt_frozen = d->d_dtfrozen;
+    d->h_ctl->dt_frozen_len = d->dtfrozen_len;
+    return write_ctl(d);
+}
+
+int lg_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask, double *J,
+               double *dJ_de0, double *dJ_dhgcoef)
+{
+    if (!d || ncycles < 1 || ckpt_k < 1 || !mask || !J || !dJ_de0 || !dJ_dhgcoef)
+        return set_error(LG_ERR_INVALID, "invalid argument");
+    if (d->opts.precision == LG_MIXED)
+        return set_error(LG_ERR_INVALID, "the adjoint differentiates the FP64 paths only");
+    int st;
+    if ((st = ensure_device(d))) return st;
+    if ((st = read_ctl(d))) return st;
+    if (d->h_ctl->status != 0) return d->h_ctl->status;
+    const int c0 = d->h_ctl->cycle;
+    if (!d->d_dtfrozen || c0 + ncycles > d->dtfrozen_len)
+        return set_error(LG_ERR_STATE, "lg_adjoint needs frozen time steps for cycles %d..%d "
+                                       "(lg_dt_freeze)", c0, c0 + ncycles - 1);
+    drop_graphs(d);  // the adjoint launches its own cycles
+    const lg::Problem &p = d->prob;
+    lg::AdjointIO io{&d->ds, d->ks, d->stream, d->h_ctl, d->h_dtfrozen.data() + c0, ncycles,
+                     ckpt_k, mask, d->ds.prm.hgcoef, &p.lxim, &p.lxip, &p.letam, &p.letap,
+                     &p.lzetam, &p.lzetap, &p.elemBC};
+    st = lg::adjoint_run(io, J, dJ_de0, dJ_dhgcoef);
+    d->launches += 10LL * ncycles;
+    return st;
 }
 
 int lg_profile(lg_domain *d, int ncycles, double *ms, const char **names, int *nkernels)

@@ -23,9 +23,15 @@ __device__ __forceinline__ void opaque(double &v) { asm volatile("" : "+d"(v)); 
 
 __device__ __forceinline__ void raise_status(Ctl *c, int code) { atomicCAS(&c->status, 0, code); }
 
-// TimeIncrement, lulesh.cc:166-222
+// TimeIncrement, lulesh.cc:166-222 (or the frozen step of this cycle)
 __device__ __forceinline__ void time_increment(Ctl *c)
 {
+    if (c->dt_frozen && c->cycle < c->dt_frozen_len) {
+        c->deltatime = c->dt_frozen[c->cycle];
+        c->time += c->deltatime;
+        ++c->cycle;
+        return;
+    }
     double targetdt = c->stoptime - c->time;
     if ((c->dtfixed <= 0.0) && (c->cycle != 0)) {
         double ratio;
@@ -48,6 +54,7 @@ __device__ __forceinline__ void time_increment(Ctl *c)
     if ((targetdt > c->deltatime) && (targetdt < (4.0 * c->deltatime / 3.0)))
         targetdt = 2.0 * c->deltatime / 3.0;
     if (targetdt < c->deltatime) c->deltatime = targetdt;
+    if (c->dt_record && c->cycle < c->dt_record_len) c->dt_record[c->cycle] = c->deltatime;
     c->time += c->deltatime;
     ++c->cycle;
 }

@@ -43,6 +43,13 @@ struct Ctl {
     int err_matvol;
     unsigned int blocks_done;
     int pad;
+    // frozen time steps: when non-null, cycle c (0-based) uses dt_frozen[c]
+    // (c < dt_frozen_len) instead of TimeIncrement's selection; dt_record[c]
+    // receives every cycle's time step when non-null (c < dt_record_len)
+    const double *dt_frozen;
+    double *dt_record;
+    int dt_frozen_len;
+    int dt_record_len;
 };
 
 struct Params {

@@ -4,7 +4,14 @@
 // R = double the code is the reference's arithmetic operation for operation.
 #pragma once
 
+#ifdef __CUDACC__
 #include <cuda_runtime.h>
+#define LG_HD __host__ __device__ __forceinline__
+#else
+#include <cmath>
+#define LG_HD inline
+using std::sqrt;
+#endif
 
 namespace lg {
 namespace geom {
@@ -15,7 +22,7 @@ namespace geom {
 
 // Jacobian determinant of CalcElemShapeFunctionDerivatives (lulesh.cc:319-376)
 template <typename R>
-__device__ __forceinline__ R jacobian_det(const R *x, const R *y, const R *z)
+LG_HD R jacobian_det(const R *x, const R *y, const R *z)
 {
     const R fjxxi = R(.125) * ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
     const R fjxet = R(.125) * ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
@@ -35,7 +42,7 @@ __device__ __forceinline__ R jacobian_det(const R *x, const R *y, const R *z)
 // CalcElemShapeFunctionDerivatives rows 0..3 of B (rows 4..7 are their
 // negatives) and the determinant, lulesh.cc:290-377
 template <typename R>
-__device__ __forceinline__ R shape_derivs(const R *x, const R *y, const R *z, R bx[4], R by[4],
+LG_HD R shape_derivs(const R *x, const R *y, const R *z, R bx[4], R by[4],
                                           R bz[4])
 {
     const R fjxxi = R(.125) * ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
@@ -73,7 +80,7 @@ __device__ __forceinline__ R shape_derivs(const R *x, const R *y, const R *z, R 
 
 // SumElemFaceNormal, lulesh.cc:381-415 (the four corners a,b,c,d of a face)
 template <typename R>
-__device__ __forceinline__ void face_normal(R *nx, R *ny, R *nz, const R *x, const R *y,
+LG_HD void face_normal(R *nx, R *ny, R *nz, const R *x, const R *y,
                                             const R *z, int a, int b, int c, int d)
 {
     const R bisectX0 = R(0.5) * (x[d] + x[c] - x[b] - x[a]);
@@ -92,7 +99,7 @@ __device__ __forceinline__ void face_normal(R *nx, R *ny, R *nz, const R *x, con
 
 // CalcElemNodeNormals, lulesh.cc:419-474
 template <typename R>
-__device__ __forceinline__ void node_normals(R *pfx, R *pfy, R *pfz, const R *x, const R *y,
+LG_HD void node_normals(R *pfx, R *pfy, R *pfz, const R *x, const R *y,
                                              const R *z)
 {
 #pragma unroll
@@ -108,7 +115,7 @@ __device__ __forceinline__ void node_normals(R *pfx, R *pfy, R *pfz, const R *x,
 // VoluDer, lulesh.cc:591-619, for corner k of CalcElemVolumeDerivative
 // (lulesh.cc:623-663) with neighbour nodes m0..m5
 template <typename R>
-__device__ __forceinline__ void volu_der(const R *x, const R *y, const R *z, int m0, int m1, int m2,
+LG_HD void volu_der(const R *x, const R *y, const R *z, int m0, int m1, int m2,
                                          int m3, int m4, int m5, R &dvdx, R &dvdy, R &dvdz)
 {
     const R twelfth = R(1.0) / R(12.0);
@@ -127,7 +134,7 @@ __device__ __forceinline__ void volu_der(const R *x, const R *y, const R *z, int
 }
 
 template <typename R>
-__device__ __forceinline__ void volume_derivative(const R *x, const R *y, const R *z, R *dvdx,
+LG_HD void volume_derivative(const R *x, const R *y, const R *z, R *dvdx,
                                                   R *dvdy, R *dvdz)
 {
     volu_der(x, y, z, 1, 2, 3, 4, 5, 7, dvdx[0], dvdy[0], dvdz[0]);
@@ -142,7 +149,7 @@ __device__ __forceinline__ void volume_derivative(const R *x, const R *y, const 
 
 // CalcElemVolume, lulesh.cc:1273-1356
 template <typename R>
-__device__ __forceinline__ R elem_volume(const R *x, const R *y, const R *z)
+LG_HD R elem_volume(const R *x, const R *y, const R *z)
 {
     const R twelveth = R(1.0) / R(12.0);
     const R dx61 = x[6] - x[1], dy61 = y[6] - y[1], dz61 = z[6] - z[1];
@@ -171,7 +178,7 @@ __device__ __forceinline__ R elem_volume(const R *x, const R *y, const R *z)
 
 // AreaFace, lulesh.cc:1370-1390
 template <typename R>
-__device__ __forceinline__ R area_face(const R *x, const R *y, const R *z, int a, int b, int c,
+LG_HD R area_face(const R *x, const R *y, const R *z, int a, int b, int c,
                                        int d)
 {
     const R fx = (x[c] - x[a]) - (x[d] - x[b]);
@@ -187,7 +194,7 @@ __device__ __forceinline__ R area_face(const R *x, const R *y, const R *z, int a
 // CalcElemCharacteristicLength, lulesh.cc:1394-1435 (std::max(a,b) is
 // (a < b) ? b : a)
 template <typename R>
-__device__ __forceinline__ R char_length(const R *x, const R *y, const R *z, R volume)
+LG_HD R char_length(const R *x, const R *y, const R *z, R volume)
 {
     R cl = R(0.0), a;
     a = area_face(x, y, z, 0, 1, 2, 3); cl = (a < cl) ? cl : a;
@@ -201,7 +208,7 @@ __device__ __forceinline__ R char_length(const R *x, const R *y, const R *z, R v
 
 // hourglass base vectors, lulesh.cc:743-776
 template <typename R = double>
-__device__ __forceinline__ constexpr R gam(int mode, int k)
+LG_HD constexpr R gam(int mode, int k)
 {
     constexpr signed char G[4][8] = {{1, 1, -1, -1, -1, -1, 1, 1},
                                      {1, -1, -1, 1, -1, 1, 1, -1},

@@ -82,6 +82,9 @@ struct orc_domain {
     /* time-step state (lulesh-init.cc:146-156) */
     double dtcourant, dthydro, dtfixed, time, deltatime, deltatimemultlb,
         deltatimemultub, dtmax, stoptime;
+    /* frozen time steps (cycle c uses dt_frozen[c]) and recorded ones */
+    double *dt_frozen, *dt_record;
+    int dt_frozen_len, dt_record_len;
 };
 
 #define ALLOC(T, n) ((T *)calloc((size_t)(n) > 0 ? (size_t)(n) : 1, sizeof(T)))
@@ -448,7 +451,7 @@ void orc_destroy(orc_domain *d)
                      &d->determ, &d->sig, &d->dvdx, &d->dvdy, &d->dvdz, &d->x8n, &d->y8n,
                      &d->z8n, &d->dxx, &d->dyy, &d->dzz, &d->delx_xi, &d->delx_eta,
                      &d->delx_zeta, &d->delv_xi, &d->delv_eta, &d->delv_zeta, &d->vnewc,
-                     &d->eos_tmp};
+                     &d->eos_tmp, &d->dt_frozen, &d->dt_record};
     for (size_t i = 0; i < sizeof(fl) / sizeof(fl[0]); ++i) free(*fl[i]);
     int **il[] = {&d->symmX, &d->symmY, &d->symmZ, &d->nodelist, &d->lxim, &d->lxip,
                   &d->letam, &d->letap, &d->lzetam, &d->lzetap, &d->elemBC,
@@ -464,9 +467,15 @@ void orc_destroy(orc_domain *d)
 /* time step                                                                 */
 /* ------------------------------------------------------------------------ */
 
-/* TimeIncrement, lulesh.cc:166-222 */
+/* TimeIncrement, lulesh.cc:166-222 (or the frozen step of this cycle) */
 static void time_increment(orc_domain *d)
 {
+    if (d->dt_frozen && d->cycle < d->dt_frozen_len) {
+        d->deltatime = d->dt_frozen[d->cycle];
+        d->time += d->deltatime;
+        ++d->cycle;
+        return;
+    }
     double targetdt = d->stoptime - d->time;
     if ((d->dtfixed <= 0.0) && (d->cycle != 0)) {
         double ratio;
@@ -489,9 +498,37 @@ static void time_increment(orc_domain *d)
     if ((targetdt > d->deltatime) && (targetdt < (4.0 * d->deltatime / 3.0)))
         targetdt = 2.0 * d->deltatime / 3.0;
     if (targetdt < d->deltatime) d->deltatime = targetdt;
+    if (d->dt_record && d->cycle < d->dt_record_len) d->dt_record[d->cycle] = d->deltatime;
     d->time += d->deltatime;
     ++d->cycle;
 }
+
+int orc_dt_freeze(orc_domain *d, const double *dts, int n)
+{
+    free(d->dt_frozen);
+    d->dt_frozen = NULL;
+    d->dt_frozen_len = 0;
+    if (n > 0) {
+        d->dt_frozen = ALLOC(double, n);
+        memcpy(d->dt_frozen, dts, sizeof(double) * (size_t)n);
+        d->dt_frozen_len = n;
+    }
+    return 0;
+}
+
+int orc_dt_record(orc_domain *d, int capacity)
+{
+    free(d->dt_record);
+    d->dt_record = NULL;
+    d->dt_record_len = 0;
+    if (capacity > 0) {
+        d->dt_record = ALLOC(double, capacity);
+        d->dt_record_len = capacity;
+    }
+    return 0;
+}
+
+const double *orc_dt_recorded(orc_domain *d) { return d->dt_record; }
 
 static inline void gather8(const orc_domain *d, const double *f, const int *en, double o[8])
 {

@@ -63,6 +63,13 @@ int    orc_set_scalar(orc_domain *d, const char *name, double value);
 /* Number of EOS repetitions for region r (lulesh.cc:2387-2401). */
 int orc_region_rep(orc_domain *d, int r);
 
+/* Frozen time steps: cycle c (0-based) uses dts[c] (c < n) instead of
+ * TimeIncrement's selection; n = 0 unfreezes.  Recording: every following
+ * cycle stores its step at index c < capacity (orc_dt_recorded). */
+int orc_dt_freeze(orc_domain *d, const double *dts, int n);
+int orc_dt_record(orc_domain *d, int capacity);
+const double *orc_dt_recorded(orc_domain *d);
+
 /* Rebuild the corner-per-node list from the current nodelist
  * (lulesh-init.cc:272-337).  Call after replacing nodelist. */
 void orc_rebuild_corner_list(orc_domain *d);

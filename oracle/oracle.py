@@ -63,6 +63,10 @@ def _port(lib_path: str = PORT_LIB) -> ctypes.CDLL:
     lib.orc_get_scalar.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.orc_set_scalar.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double]
     lib.orc_region_rep.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.orc_dt_freeze.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    lib.orc_dt_record.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.orc_dt_recorded.restype = ctypes.POINTER(ctypes.c_double)
+    lib.orc_dt_recorded.argtypes = [ctypes.c_void_p]
     return lib
 
 
@@ -114,6 +118,16 @@ class OracleDomain:
 
     def region_rep(self, r: int) -> int:
         return self._lib.orc_region_rep(self._h, r)
+
+    def dt_freeze(self, dts) -> None:
+        a = np.ascontiguousarray(dts, dtype=np.float64)
+        self._lib.orc_dt_freeze(self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), a.size)
+
+    def dt_record(self, capacity: int) -> None:
+        self._lib.orc_dt_record(self._h, capacity)
+
+    def dt_recorded(self, n: int) -> np.ndarray:
+        return np.ctypeslib.as_array(self._lib.orc_dt_recorded(self._h), shape=(n,)).copy()
 
     def state(self) -> dict:
         out = {f: self.field(f).copy() for f in NODE_FIELDS + ELEM_FIELDS}

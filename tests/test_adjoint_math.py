@@ -1,0 +1,53 @@
+"""Element-local vector-Jacobian products of the adjoint (lg_adjoint_math.h),
+checked on the host against central finite differences of the forward
+formulas, for random elements, every branch of the limiter and both signs of
+the volume change in the EOS."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_element_vjps_match_finite_differences(tmp_path):
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    exe = tmp_path / "adjoint_selftest"
+    subprocess.run(["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "lulesh_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "adjoint_selftest.cc"), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    worst = float(r.stdout.strip().splitlines()[-1].split()[-1])
+    assert r.returncode == 0 and worst < 1e-6, r.stdout[-2000:]
+
+
+def test_whole_cycle_adjoint_matches_finite_differences(tmp_path):
+    """lg_adjoint_cycle.h's item functions -- the GPU adjoint kernels' code --
+    looped on the host over oracle states, against oracle finite differences
+    (relative step 1e-7)."""
+    if not shutil.which("g++") or not shutil.which("gcc"):
+        pytest.skip("no host compilers")
+    obj = tmp_path / "orc.o"
+    exe = tmp_path / "adjoint_cycle_selftest"
+    subprocess.run(["gcc", "-O1", "-std=c11", "-ffp-contract=off", "-c",
+                    os.path.join(ROOT, "oracle", "lulesh_oracle.c"), "-o", str(obj)], check=True)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "lulesh_gb300", "csrc"),
+                    "-I", os.path.join(ROOT, "oracle"),
+                    os.path.join(ROOT, "tests", "adjoint_cycle_selftest.cc"), str(obj), "-o",
+                    str(exe)], check=True)
+    # each line must agree at relative step 1e-6 or 1e-7: the larger step
+    # carries truncation error on these small meshes, the smaller round-off
+    worst = {}
+    for rel in ("1e-6", "1e-7"):
+        env = dict(os.environ, LG_FD_REL=rel)
+        for args in (["6", "5", "216"], ["12", "40", "40"], ["20", "60", "200"]):
+            r = subprocess.run([str(exe)] + args, capture_output=True, text=True, env=env)
+            assert r.returncode == 0, r.stdout + r.stderr
+            # random directions and hgcoef (the single-element probes of cold
+            # elements sit on the sound-speed floor and are reported only)
+            for l in r.stdout.splitlines():
+                if l.startswith(("e0 dir 3", "e0 dir 4", "e0 dir 5", "hgcoef")):
+                    key = (tuple(args), l.split(":")[0])
+                    worst[key] = min(worst.get(key, 1.0), float(l.split()[-1]))
+    assert len(worst) == 12 and max(worst.values()) < 1e-6, worst
