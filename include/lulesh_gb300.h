@@ -163,8 +163,11 @@ int lg_dt_freeze(lg_domain *d, const double *dts, int n);
  * The time steps must be frozen for these cycles (lg_dt_freeze).  Runs the
  * forward cycles with a checkpoint every ckpt_k cycles, recomputes each
  * segment and sweeps it backwards; leaves the handle in the final state and
- * returns *J.  Non-smooth operations (cut-offs, clamps, the monotonic
- * limiter) contribute the derivative of the branch taken.  FP64 paths only. */
+ * returns *J.  Non-smooth operations: the physical clamps and switches
+ * (emin, pmin, eosvmin/eosvmax, the monotonic limiter, vdov > 0, delvc > 0,
+ * the sound-speed floors) contribute the derivative of the branch taken; the
+ * noise cut-offs (u_cut, p_cut, e_cut, q_cut, v_cut) pass it through.
+ * FP64 paths only (LG_FP64, LG_FP64_FMA). */
 int lg_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask, double *J,
                double *dJ_de0, double *dJ_dhgcoef);
 

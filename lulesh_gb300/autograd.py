@@ -19,23 +19,30 @@ class TerminalEnergyProblem:
     """A Sedov problem, a cycle count, a frozen dt sequence and an element mask.
 
     The dt sequence and the mask come from one forward run of `e_base`
-    (the mask: element centroids within `radius` of the origin at the end)."""
+    (the mask: element centroids within `radius` of the origin at the end),
+    unless given (`dts`: ncycles steps; `mask`: numElem booleans)."""
 
     def __init__(self, nx: int = 48, numReg: int = 11, ncycles: int = 200, ckpt: int = 20,
                  e_base: np.ndarray | None = None, radius: float = 0.5,
-                 precision: str = "fp64", device: int = 0):
+                 precision: str = "fp64", device: int = 0, dts: np.ndarray | None = None,
+                 mask: np.ndarray | None = None):
         self.nx, self.ncycles, self.ckpt = nx, ncycles, ckpt
         self.dom = Domain(nx, numReg, its=10 ** 9, precision=precision, device=device)
         self.e_init = self.dom.field("e")
         self.e_base = self.e_init.copy() if e_base is None else np.asarray(e_base, np.float64)
         self.hg_base = self.dom.scalar("hgcoef")
-        self.dom.set_field("e", self.e_base)
-        self.dom.dt_record(ncycles)
-        if self.dom.step(ncycles) != 0:
-            raise RuntimeError("forward run failed")
-        self.dts = self.dom.dt_get(ncycles)
-        self.mask = centroid_mask(self.dom, radius)
-        self.dom.dt_record(0)
+        if dts is None or mask is None:
+            self.dom.set_field("e", self.e_base)
+            self.dom.dt_record(ncycles)
+            if self.dom.step(ncycles) != 0:
+                raise RuntimeError("forward run failed")
+            rec_dts = self.dom.dt_get(ncycles)
+            rec_mask = centroid_mask(self.dom, radius)
+            self.dom.dt_record(0)
+        self.dts = np.asarray(dts, np.float64) if dts is not None else rec_dts
+        self.mask = np.asarray(mask, bool) if mask is not None else rec_mask
+        if self.dts.size != ncycles or self.mask.size != self.e_init.size:
+            raise ValueError("dts must hold ncycles steps and mask one flag per element")
         self.dom.dt_freeze(self.dts)
 
     def objective(self, e0: np.ndarray, hgcoef: float) -> float:

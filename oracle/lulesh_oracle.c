@@ -17,16 +17,29 @@
  *    constraints) run per region exactly as the reference does, but errors
  *    are returned as status codes instead of exit().
  */
-#include "lulesh_oracle.h"
-
 #include <limits.h>
 #include <math.h>
+#include <stddef.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
+#ifdef ORC_LONG_DOUBLE
+/* The extended-precision build (liblulesh_oracle_tape_ld.so, a reference for
+ * finite differences only): every double of this file and of its API becomes
+ * long double, with the long double forms of the math functions.  Not a
+ * parity build: its results differ from the reference's in the last bits of
+ * double precision. */
+#define sqrt sqrtl
+#define cbrt cbrtl
+#define fabs fabsl
+#define pow powl
+#define double long double
+#endif
+#include "lulesh_oracle.h"
 
 /* element face boundary-condition bits (lulesh.h:59-87) */
 #define XI_M 0x00007
@@ -85,9 +98,283 @@ struct orc_domain {
     /* frozen time steps (cycle c uses dt_frozen[c]) and recorded ones */
     double *dt_frozen, *dt_record;
     int dt_frozen_len, dt_record_len;
+    /* decision tape (ORC_TAPE builds only; NULL otherwise) */
+    struct orc_tape_state *tape;
 };
 
 #define ALLOC(T, n) ((T *)calloc((size_t)(n) > 0 ? (size_t)(n) : 1, sizeof(T)))
+
+/* ------------------------------------------------------------------------ */
+/* decision tape                                                             */
+/* ------------------------------------------------------------------------ */
+/*
+ * Built with -DORC_TAPE only (liblulesh_oracle_tape.so); every other build
+ * compiles the TAPE_IF / TAPE_CUT sites below to the plain comparisons of
+ * the reference, so its arithmetic is unchanged.
+ *
+ * Record mode stores, per cycle, the outcome of every branch of the cycle
+ * that can change a state value (the monotonic limiter's min/max and its
+ * vdov and delv*delx switches, the eosvmin/eosvmax clamps of vnewc and of
+ * the EOS, the delvc > 0 switches, the emin and pmin clamps, the sound-speed
+ * floors) and, for each noise cut-off that fired (|u| < u_cut, |p| < p_cut,
+ * |e| < e_cut, |q| < q_cut, |v - 1| < v_cut), the offset it applied.  Replay
+ * mode takes the recorded outcomes instead of evaluating the comparisons and
+ * adds the recorded offsets where a cut-off fired.  Replayed cycles are a
+ * smooth function of the state (compositions of +, *, / and sqrt), equal to
+ * the plain cycles bitwise at the recorded trajectory: central differences
+ * of a replay resolve the derivative of the branch the recorded run took,
+ * the derivative with clamps and switches held and noise cut-offs passed.
+ * The Courant/hydro constraints (which only choose time steps) and the error
+ * checks are not taped.
+ */
+enum {
+    TB_PHI = 0,        /* 3 directions x 4 limiter comparisons: bits 0-11 */
+    TB_VDOV = 12,      /* vdov > 0 */
+    TB_DELVX = 13,     /* delv*delx > 0, 3 directions: bits 13-15 */
+    TB_VC_MIN = 16, TB_VC_MAX = 17,          /* vnewc clamps */
+    TB_EOS_VMIN = 18, TB_EOS_VMAX = 19,      /* EOS compression switches */
+    TB_E1_EMIN = 20,
+    TB_P_HALF = 21,    /* p_cut, eosvmax, pmin of the half-step pressure: 21-23 */
+    TB_Q1_COMP = 24, TB_Q1_FLOOR = 25, TB_E3_CUT = 26, TB_E3_EMIN = 27,
+    TB_P_NEW1 = 28,    /* 28-30 */
+    TB_QT_COMP = 31, TB_QT_FLOOR = 32, TB_E4_CUT = 33, TB_E4_EMIN = 34,
+    TB_P_NEW2 = 35,    /* 35-37 */
+    TB_QF_COMP = 38, TB_QF_FLOOR = 39, TB_QF_CUT = 40, TB_SS_FLOOR = 41, TB_V_CUT = 42,
+    TB_NODE_U = 0      /* node bits: u_cut of xd, yd, zd: 0-2 */
+};
+/* slots of the cut-off offsets: 0-6 element sites, 7-9 node sites */
+enum {
+    TS_P_HALF, TS_E3, TS_P_NEW1, TS_E4, TS_P_NEW2, TS_QF, TS_V, TS_U, TS_NSLOT = TS_U + 3
+};
+
+#ifdef ORC_TAPE
+struct orc_tape_data {
+    int ncyc, E, N;
+    uint64_t *eb;      /* ncyc x E decision bits */
+    uint8_t *nb;       /* ncyc x N decision bits */
+    size_t *off_start; /* ncyc + 1: offsets of cycle c in [off_start[c], off_start[c+1]) */
+    int *off_slot, *off_idx;
+    double *off_val;
+    size_t off_len, off_cap;
+};
+
+struct orc_tape_state {
+    int mode; /* 1 record, 2 replay */
+    int next; /* tape cycle of the next orc_step cycle */
+    int cyc;  /* tape cycle running, -1 outside */
+    struct orc_tape_data *data;
+    int owns;
+    double *dense[TS_NSLOT];
+};
+
+static inline int tape_bit_e(const orc_domain *d, int bit, int idx, int cond)
+{
+    const struct orc_tape_state *t = d->tape;
+    if (!t || t->cyc < 0) return cond;
+    uint64_t *w = &t->data->eb[(size_t)t->cyc * t->data->E + idx];
+    if (t->mode == 1) {
+        if (cond) *w |= (uint64_t)1 << bit;
+        return cond;
+    }
+    return (int)((*w >> bit) & 1u);
+}
+
+static inline int tape_bit_n(const orc_domain *d, int bit, int idx, int cond)
+{
+    const struct orc_tape_state *t = d->tape;
+    if (!t || t->cyc < 0) return cond;
+    uint8_t *w = &t->data->nb[(size_t)t->cyc * t->data->N + idx];
+    if (t->mode == 1) {
+        if (cond) *w |= (uint8_t)(1u << bit);
+        return cond;
+    }
+    return (int)((*w >> bit) & 1u);
+}
+
+/* a noise cut-off "x = target when cond": record the offset, replay it */
+static inline double tape_cut(const orc_domain *d, int node, int bit, int slot, int idx,
+                              double x, int cond, double target)
+{
+    const struct orc_tape_state *t = d->tape;
+    if (!t || t->cyc < 0) return cond ? target : x;
+    const int fired = node ? tape_bit_n(d, bit, idx, cond) : tape_bit_e(d, bit, idx, cond);
+    if (!fired) return x;
+    if (t->mode == 1) {
+        t->dense[slot][idx] = target - x;
+        return target;
+    }
+    return x + t->dense[slot][idx];
+}
+
+#define TAPE_IF(bit, idx, cond) tape_bit_e(d, (bit), (idx), (cond))
+#define TAPE_CUT(bit, slot, idx, x, cond, target) \
+    tape_cut(d, 0, (bit), (slot), (idx), (x), (cond), (target))
+#define TAPE_CUT_NODE(bit, slot, idx, x, cond, target) \
+    tape_cut(d, 1, (bit), (slot), (idx), (x), (cond), (target))
+
+static void tape_free(struct orc_tape_state *t)
+{
+    if (!t) return;
+    if (t->owns && t->data) {
+        free(t->data->eb);
+        free(t->data->nb);
+        free(t->data->off_start);
+        free(t->data->off_slot);
+        free(t->data->off_idx);
+        free(t->data->off_val);
+        free(t->data);
+    }
+    for (int k = 0; k < TS_NSLOT; ++k) free(t->dense[k]);
+    free(t);
+}
+
+static struct orc_tape_state *tape_new(const orc_domain *d)
+{
+    struct orc_tape_state *t = (struct orc_tape_state *)calloc(1, sizeof(*t));
+    if (!t) return NULL;
+    for (int k = 0; k < TS_NSLOT; ++k) {
+        const int n = k >= TS_U ? d->numNode : d->numElem;
+        t->dense[k] = (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+        if (!t->dense[k]) {
+            tape_free(t);
+            return NULL;
+        }
+    }
+    t->cyc = -1;
+    return t;
+}
+
+static void tape_begin_cycle(orc_domain *d)
+{
+    struct orc_tape_state *t = d->tape;
+    if (!t) return;
+    struct orc_tape_data *D = t->data;
+    if (t->next >= D->ncyc) {
+        t->cyc = -1;
+        return;
+    }
+    t->cyc = t->next;
+    const size_t c = (size_t)t->cyc;
+    if (t->mode == 1) {
+        memset(D->eb + c * D->E, 0, sizeof(uint64_t) * (size_t)D->E);
+        memset(D->nb + c * D->N, 0, (size_t)D->N);
+        D->off_start[c] = D->off_len;
+    } else {
+        for (size_t k = D->off_start[c]; k < D->off_start[c + 1]; ++k)
+            t->dense[D->off_slot[k]][D->off_idx[k]] = D->off_val[k];
+    }
+}
+
+static int tape_push(struct orc_tape_data *D, int slot, int idx, double val)
+{
+    if (D->off_len == D->off_cap) {
+        const size_t cap = D->off_cap ? 2 * D->off_cap : 4096;
+        int *s2 = (int *)realloc(D->off_slot, cap * sizeof(int));
+        if (s2) D->off_slot = s2;
+        int *i2 = (int *)realloc(D->off_idx, cap * sizeof(int));
+        if (i2) D->off_idx = i2;
+        double *v2 = (double *)realloc(D->off_val, cap * sizeof(double));
+        if (v2) D->off_val = v2;
+        if (!s2 || !i2 || !v2) return -1;
+        D->off_cap = cap;
+    }
+    D->off_slot[D->off_len] = slot;
+    D->off_idx[D->off_len] = idx;
+    D->off_val[D->off_len] = val;
+    ++D->off_len;
+    return 0;
+}
+
+static void tape_end_cycle(orc_domain *d)
+{
+    struct orc_tape_state *t = d->tape;
+    if (!t || t->cyc < 0) return;
+    struct orc_tape_data *D = t->data;
+    const size_t c = (size_t)t->cyc;
+    if (t->mode == 1) {
+        static const int ebit[TS_U] = {TB_P_HALF, TB_E3_CUT, TB_P_NEW1, TB_E4_CUT,
+                                       TB_P_NEW2, TB_QF_CUT, TB_V_CUT};
+        const uint64_t *eb = D->eb + c * D->E;
+        const uint8_t *nb = D->nb + c * D->N;
+        for (int k = 0; k < TS_U; ++k)
+            for (int i = 0; i < D->E; ++i)
+                if (((eb[i] >> ebit[k]) & 1u) && t->dense[k][i] != 0.0)
+                    tape_push(D, k, i, t->dense[k][i]);
+        for (int k = 0; k < 3; ++k)
+            for (int i = 0; i < D->N; ++i)
+                if (((nb[i] >> (TB_NODE_U + k)) & 1u) && t->dense[TS_U + k][i] != 0.0)
+                    tape_push(D, TS_U + k, i, t->dense[TS_U + k][i]);
+        D->off_start[c + 1] = D->off_len;
+    } else {
+        for (size_t k = D->off_start[c]; k < D->off_start[c + 1]; ++k)
+            t->dense[D->off_slot[k]][D->off_idx[k]] = 0.0;
+    }
+    t->cyc = -1;
+    ++t->next;
+}
+
+int orc_tape_record(orc_domain *d, int ncycles)
+{
+    tape_free(d->tape);
+    d->tape = NULL;
+    if (ncycles <= 0) return 0;
+    struct orc_tape_state *t = tape_new(d);
+    struct orc_tape_data *D = (struct orc_tape_data *)calloc(1, sizeof(*D));
+    if (!t || !D) {
+        free(D);
+        tape_free(t);
+        return -1;
+    }
+    t->data = D;
+    t->owns = 1;
+    t->mode = 1;
+    D->ncyc = ncycles;
+    D->E = d->numElem;
+    D->N = d->numNode;
+    D->eb = (uint64_t *)calloc((size_t)ncycles * (size_t)(D->E > 0 ? D->E : 1), sizeof(uint64_t));
+    D->nb = (uint8_t *)calloc((size_t)ncycles * (size_t)(D->N > 0 ? D->N : 1), 1);
+    D->off_start = (size_t *)calloc((size_t)ncycles + 1, sizeof(size_t));
+    if (!D->eb || !D->nb || !D->off_start) {
+        tape_free(t);
+        return -1;
+    }
+    d->tape = t;
+    return 0;
+}
+
+int orc_tape_replay(orc_domain *d, const orc_domain *src)
+{
+    tape_free(d->tape);
+    d->tape = NULL;
+    if (!src || !src->tape || src->tape->mode != 1) return -1;
+    if (src->numElem != d->numElem || src->numNode != d->numNode) return -1;
+    struct orc_tape_state *t = tape_new(d);
+    if (!t) return -1;
+    t->data = src->tape->data;
+    t->owns = 0;
+    t->mode = 2;
+    d->tape = t;
+    return 0;
+}
+
+int orc_tape_stop(orc_domain *d)
+{
+    tape_free(d->tape);
+    d->tape = NULL;
+    return 0;
+}
+#else
+struct orc_tape_state;
+#define TAPE_IF(bit, idx, cond) (cond)
+#define TAPE_CUT(bit, slot, idx, x, cond, target) ((cond) ? (target) : (x))
+#define TAPE_CUT_NODE(bit, slot, idx, x, cond, target) ((cond) ? (target) : (x))
+static inline void tape_free(struct orc_tape_state *t) { (void)t; }
+static inline void tape_begin_cycle(orc_domain *d) { (void)d; }
+static inline void tape_end_cycle(orc_domain *d) { (void)d; }
+int orc_tape_record(orc_domain *d, int ncycles) { (void)d; (void)ncycles; return -1; }
+int orc_tape_replay(orc_domain *d, const orc_domain *src) { (void)d; (void)src; return -1; }
+int orc_tape_stop(orc_domain *d) { (void)d; return -1; }
+#endif
 
 /* ------------------------------------------------------------------------ */
 /* setup: Domain::Domain and helpers (lulesh-init.cc)                        */
@@ -460,6 +747,7 @@ void orc_destroy(orc_domain *d)
     for (int r = 0; r < d->numReg; ++r) free(d->regElemlist[r]);
     free(d->regElemlist);
     for (size_t i = 0; i < sizeof(il) / sizeof(il[0]); ++i) free(*il[i]);
+    tape_free(d->tape);
     free(d);
 }
 
@@ -842,13 +1130,13 @@ static int lagrange_nodal(orc_domain *d)
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < N; ++i) {
         double xdtmp = d->xd[i] + d->xdd[i] * delt;
-        if (fabs(xdtmp) < u_cut) xdtmp = 0.0;
+        xdtmp = TAPE_CUT_NODE(TB_NODE_U + 0, TS_U + 0, i, xdtmp, fabs(xdtmp) < u_cut, 0.0);
         d->xd[i] = xdtmp;
         double ydtmp = d->yd[i] + d->ydd[i] * delt;
-        if (fabs(ydtmp) < u_cut) ydtmp = 0.0;
+        ydtmp = TAPE_CUT_NODE(TB_NODE_U + 1, TS_U + 1, i, ydtmp, fabs(ydtmp) < u_cut, 0.0);
         d->yd[i] = ydtmp;
         double zdtmp = d->zd[i] + d->zdd[i] * delt;
-        if (fabs(zdtmp) < u_cut) zdtmp = 0.0;
+        zdtmp = TAPE_CUT_NODE(TB_NODE_U + 2, TS_U + 2, i, zdtmp, fabs(zdtmp) < u_cut, 0.0);
         d->zd[i] = zdtmp;
     }
 #pragma omp parallel for schedule(static)
@@ -1014,8 +1302,9 @@ static void monoq_gradients(orc_domain *d)
 /* one direction of the monotonic limiter, lulesh.cc:1778-1813 */
 static double monoq_phi(const orc_domain *d, const double *delv_dir, int ielem, int bc,
                         int mmask, int msymm, int mfree, int mcomm, int pmask, int psymm,
-                        int pfree, int pcomm, int nbm, int nbp, double ptiny)
+                        int pfree, int pcomm, int nbm, int nbp, double ptiny, int bit0)
 {
+    (void)bit0;
     double delvm = 0.0, delvp = 0.0;
     double norm = 1. / (delv_dir[ielem] + ptiny);
     int bm = bc & mmask;
@@ -1041,10 +1330,10 @@ static double monoq_phi(const orc_domain *d, const double *delv_dir, int ielem, 
     double phi = .5 * (delvm + delvp);
     delvm *= d->monoq_limiter_mult;
     delvp *= d->monoq_limiter_mult;
-    if (delvm < phi) phi = delvm;
-    if (delvp < phi) phi = delvp;
-    if (phi < 0.) phi = 0.;
-    if (phi > d->monoq_max_slope) phi = d->monoq_max_slope;
+    if (TAPE_IF(bit0 + 0, ielem, delvm < phi)) phi = delvm;
+    if (TAPE_IF(bit0 + 1, ielem, delvp < phi)) phi = delvp;
+    if (TAPE_IF(bit0 + 2, ielem, phi < 0.)) phi = 0.;
+    if (TAPE_IF(bit0 + 3, ielem, phi > d->monoq_max_slope)) phi = d->monoq_max_slope;
     return phi;
 }
 
@@ -1061,24 +1350,24 @@ static void monoq_region(orc_domain *d, int r)
         double qlin, qquad;
         double phixi = monoq_phi(d, d->delv_xi, ielem, bc, XI_M, XI_M_SYMM, XI_M_FREE,
                                  XI_M_COMM, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM,
-                                 d->lxim[ielem], d->lxip[ielem], ptiny);
+                                 d->lxim[ielem], d->lxip[ielem], ptiny, TB_PHI + 0);
         double phieta = monoq_phi(d, d->delv_eta, ielem, bc, ETA_M, ETA_M_SYMM, ETA_M_FREE,
                                   ETA_M_COMM, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM,
-                                  d->letam[ielem], d->letap[ielem], ptiny);
+                                  d->letam[ielem], d->letap[ielem], ptiny, TB_PHI + 4);
         double phizeta = monoq_phi(d, d->delv_zeta, ielem, bc, ZETA_M, ZETA_M_SYMM,
                                    ZETA_M_FREE, ZETA_M_COMM, ZETA_P, ZETA_P_SYMM,
                                    ZETA_P_FREE, ZETA_P_COMM, d->lzetam[ielem],
-                                   d->lzetap[ielem], ptiny);
-        if (d->vdov[ielem] > 0.) {
+                                   d->lzetap[ielem], ptiny, TB_PHI + 8);
+        if (TAPE_IF(TB_VDOV, ielem, d->vdov[ielem] > 0.)) {
             qlin = 0.;
             qquad = 0.;
         } else {
             double delvxxi = d->delv_xi[ielem] * d->delx_xi[ielem];
             double delvxeta = d->delv_eta[ielem] * d->delx_eta[ielem];
             double delvxzeta = d->delv_zeta[ielem] * d->delx_zeta[ielem];
-            if (delvxxi > 0.) delvxxi = 0.;
-            if (delvxeta > 0.) delvxeta = 0.;
-            if (delvxzeta > 0.) delvxzeta = 0.;
+            if (TAPE_IF(TB_DELVX + 0, ielem, delvxxi > 0.)) delvxxi = 0.;
+            if (TAPE_IF(TB_DELVX + 1, ielem, delvxeta > 0.)) delvxeta = 0.;
+            if (TAPE_IF(TB_DELVX + 2, ielem, delvxzeta > 0.)) delvxzeta = 0.;
             double rho = d->elemMass[ielem] / (d->volo[ielem] * d->vnew[ielem]);
             qlin = -d->qlc_monoq * rho *
                    (delvxxi * (1. - phixi) + delvxeta * (1. - phieta) +
@@ -1106,10 +1395,12 @@ static int calc_q(orc_domain *d)
 }
 
 /* CalcPressureForElems, lulesh.cc:2014-2044 */
-static void calc_pressure(double *p_new, double *bvc, double *pbvc, const double *e_old,
-                          const double *compression, const double *vnewc, double pmin,
-                          double p_cut, double eosvmax, int length, const int *list)
+static void calc_pressure(const orc_domain *d, int bit0, int slot, double *p_new, double *bvc,
+                          double *pbvc, const double *e_old, const double *compression,
+                          const double *vnewc, double pmin, double p_cut, double eosvmax,
+                          int length, const int *list)
 {
+    (void)d; (void)bit0; (void)slot;
     for (int i = 0; i < length; ++i) {
         const double c1s = 2.0 / 3.0;
         bvc[i] = c1s * (compression[i] + 1.);
@@ -1118,18 +1409,19 @@ static void calc_pressure(double *p_new, double *bvc, double *pbvc, const double
     for (int i = 0; i < length; ++i) {
         const int ielem = list[i];
         p_new[i] = bvc[i] * e_old[i];
-        if (fabs(p_new[i]) < p_cut) p_new[i] = 0.0;
-        if (vnewc[ielem] >= eosvmax) p_new[i] = 0.0;
-        if (p_new[i] < pmin) p_new[i] = pmin;
+        p_new[i] = TAPE_CUT(bit0 + 0, slot, ielem, p_new[i], fabs(p_new[i]) < p_cut, 0.0);
+        if (TAPE_IF(bit0 + 1, ielem, vnewc[ielem] >= eosvmax)) p_new[i] = 0.0;
+        if (TAPE_IF(bit0 + 2, ielem, p_new[i] < pmin)) p_new[i] = pmin;
     }
 }
 
 /* sound-speed-like term shared by lulesh.cc:2083-2090, 2126-2133,
  * 2158-2165, 2190-2197 */
-static inline double ssc_of(double x, double rho0)
+static inline double ssc_of(const orc_domain *d, int bit, int idx, double x, double rho0)
 {
+    (void)d; (void)bit; (void)idx;
     double ssc = x / rho0;
-    if (ssc <= .1111111e-36)
+    if (TAPE_IF(bit, idx, ssc <= .1111111e-36))
         ssc = .3333333e-18;
     else
         ssc = sqrt(ssc);
@@ -1172,10 +1464,11 @@ static void eval_eos_chunk(orc_domain *d, const int *list, int lo, int hi, int r
         }
         if (eosvmin != 0.)
             for (int i = 0; i < len; ++i)
-                if (vnewc[rl[i]] <= eosvmin) compHalfStep[i] = compression[i];
+                if (TAPE_IF(TB_EOS_VMIN, rl[i], vnewc[rl[i]] <= eosvmin))
+                    compHalfStep[i] = compression[i];
         if (eosvmax != 0.)
             for (int i = 0; i < len; ++i)
-                if (vnewc[rl[i]] >= eosvmax) {
+                if (TAPE_IF(TB_EOS_VMAX, rl[i], vnewc[rl[i]] >= eosvmax)) {
                     p_old[i] = 0.;
                     compression[i] = 0.;
                     compHalfStep[i] = 0.;
@@ -1185,16 +1478,19 @@ static void eval_eos_chunk(orc_domain *d, const int *list, int lo, int hi, int r
         /* CalcEnergyForElems, lulesh.cc:2048-2176 */
         for (int i = 0; i < len; ++i) {
             e_new[i] = e_old[i] - .5 * delvc[i] * (p_old[i] + q_old[i]) + .5 * work[i];
-            if (e_new[i] < emin) e_new[i] = emin;
+            if (TAPE_IF(TB_E1_EMIN, rl[i], e_new[i] < emin)) e_new[i] = emin;
         }
-        calc_pressure(pHalfStep, bvc, pbvc, e_new, compHalfStep, vnewc, pmin, p_cut, eosvmax,
-                      len, rl);
+        calc_pressure(d, TB_P_HALF, TS_P_HALF, pHalfStep, bvc, pbvc, e_new, compHalfStep, vnewc,
+                      pmin, p_cut, eosvmax, len, rl);
         for (int i = 0; i < len; ++i) {
+            const int ielem = rl[i];
+            (void)ielem;
             double vhalf = 1. / (1. + compHalfStep[i]);
-            if (delvc[i] > 0.) {
+            if (TAPE_IF(TB_Q1_COMP, ielem, delvc[i] > 0.)) {
                 q_new[i] = 0.;
             } else {
-                double ssc = ssc_of(pbvc[i] * e_new[i] + vhalf * vhalf * bvc[i] * pHalfStep[i],
+                double ssc = ssc_of(d, TB_Q1_FLOOR, ielem,
+                                    pbvc[i] * e_new[i] + vhalf * vhalf * bvc[i] * pHalfStep[i],
                                     rho0);
                 q_new[i] = (ssc * ql_old[i] + qq_old[i]);
             }
@@ -1203,20 +1499,23 @@ static void eval_eos_chunk(orc_domain *d, const int *list, int lo, int hi, int r
                                        4.0 * (pHalfStep[i] + q_new[i]));
         }
         for (int i = 0; i < len; ++i) {
+            const int ielem = rl[i];
+            (void)ielem;
             e_new[i] += .5 * work[i];
-            if (fabs(e_new[i]) < e_cut) e_new[i] = 0.;
-            if (e_new[i] < emin) e_new[i] = emin;
+            e_new[i] = TAPE_CUT(TB_E3_CUT, TS_E3, ielem, e_new[i], fabs(e_new[i]) < e_cut, 0.);
+            if (TAPE_IF(TB_E3_EMIN, ielem, e_new[i] < emin)) e_new[i] = emin;
         }
-        calc_pressure(p_new, bvc, pbvc, e_new, compression, vnewc, pmin, p_cut, eosvmax, len,
-                      rl);
+        calc_pressure(d, TB_P_NEW1, TS_P_NEW1, p_new, bvc, pbvc, e_new, compression, vnewc, pmin,
+                      p_cut, eosvmax, len, rl);
         for (int i = 0; i < len; ++i) {
             const double sixth = 1.0 / 6.0;
             const int ielem = rl[i];
             double q_tilde;
-            if (delvc[i] > 0.) {
+            if (TAPE_IF(TB_QT_COMP, ielem, delvc[i] > 0.)) {
                 q_tilde = 0.;
             } else {
-                double ssc = ssc_of(pbvc[i] * e_new[i] +
+                double ssc = ssc_of(d, TB_QT_FLOOR, ielem,
+                                    pbvc[i] * e_new[i] +
                                         vnewc[ielem] * vnewc[ielem] * bvc[i] * p_new[i],
                                     rho0);
                 q_tilde = (ssc * ql_old[i] + qq_old[i]);
@@ -1224,19 +1523,20 @@ static void eval_eos_chunk(orc_domain *d, const int *list, int lo, int hi, int r
             e_new[i] = e_new[i] - (7.0 * (p_old[i] + q_old[i]) -
                                    8.0 * (pHalfStep[i] + q_new[i]) + (p_new[i] + q_tilde)) *
                                       delvc[i] * sixth;
-            if (fabs(e_new[i]) < e_cut) e_new[i] = 0.;
-            if (e_new[i] < emin) e_new[i] = emin;
+            e_new[i] = TAPE_CUT(TB_E4_CUT, TS_E4, ielem, e_new[i], fabs(e_new[i]) < e_cut, 0.);
+            if (TAPE_IF(TB_E4_EMIN, ielem, e_new[i] < emin)) e_new[i] = emin;
         }
-        calc_pressure(p_new, bvc, pbvc, e_new, compression, vnewc, pmin, p_cut, eosvmax, len,
-                      rl);
+        calc_pressure(d, TB_P_NEW2, TS_P_NEW2, p_new, bvc, pbvc, e_new, compression, vnewc, pmin,
+                      p_cut, eosvmax, len, rl);
         for (int i = 0; i < len; ++i) {
             const int ielem = rl[i];
-            if (delvc[i] <= 0.) {
-                double ssc = ssc_of(pbvc[i] * e_new[i] +
+            if (TAPE_IF(TB_QF_COMP, ielem, delvc[i] <= 0.)) {
+                double ssc = ssc_of(d, TB_QF_FLOOR, ielem,
+                                    pbvc[i] * e_new[i] +
                                         vnewc[ielem] * vnewc[ielem] * bvc[i] * p_new[i],
                                     rho0);
                 q_new[i] = (ssc * ql_old[i] + qq_old[i]);
-                if (fabs(q_new[i]) < q_cut) q_new[i] = 0.;
+                q_new[i] = TAPE_CUT(TB_QF_CUT, TS_QF, ielem, q_new[i], fabs(q_new[i]) < q_cut, 0.);
             }
         }
     }
@@ -1248,7 +1548,8 @@ static void eval_eos_chunk(orc_domain *d, const int *list, int lo, int hi, int r
     }
     for (int i = 0; i < len; ++i) {
         const int ielem = rl[i];
-        d->ss[ielem] = ssc_of(pbvc[i] * e_new[i] + vnewc[ielem] * vnewc[ielem] * bvc[i] * p_new[i],
+        d->ss[ielem] = ssc_of(d, TB_SS_FLOOR, ielem,
+                              pbvc[i] * e_new[i] + vnewc[ielem] * vnewc[ielem] * bvc[i] * p_new[i],
                               rho0);
     }
 }
@@ -1271,8 +1572,8 @@ static int apply_material(orc_domain *d)
 #pragma omp parallel for schedule(static) reduction(| : bad)
     for (int i = 0; i < E; ++i) {
         double vc = d->vnew[i];
-        if (eosvmin != 0. && vc < eosvmin) vc = eosvmin;
-        if (eosvmax != 0. && vc > eosvmax) vc = eosvmax;
+        if (eosvmin != 0. && TAPE_IF(TB_VC_MIN, i, vc < eosvmin)) vc = eosvmin;
+        if (eosvmax != 0. && TAPE_IF(TB_VC_MAX, i, vc > eosvmax)) vc = eosvmax;
         d->vnewc[i] = vc;
         double v = d->v[i];
         if (eosvmin != 0. && v < eosvmin) v = eosvmin;
@@ -1307,7 +1608,7 @@ static void update_volumes(orc_domain *d)
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < E; ++i) {
         double tmpV = d->vnew[i];
-        if (fabs(tmpV - 1.0) < v_cut) tmpV = 1.0;
+        tmpV = TAPE_CUT(TB_V_CUT, TS_V, i, tmpV, fabs(tmpV - 1.0) < v_cut, 1.0);
         d->v[i] = tmpV;
     }
 }
@@ -1375,12 +1676,14 @@ int orc_phase(orc_domain *d, int phase)
 int orc_step(orc_domain *d, int ncycles)
 {
     for (int c = 0; c < ncycles && d->time < d->stoptime; ++c) {
+        tape_begin_cycle(d);
         time_increment(d);
         int st = lagrange_nodal(d);
         if (st) return st;
         st = lagrange_elements(d);
         if (st) return st;
         time_constraints(d);
+        tape_end_cycle(d);
     }
     return ORC_OK;
 }

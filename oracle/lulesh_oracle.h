@@ -70,6 +70,21 @@ int orc_dt_freeze(orc_domain *d, const double *dts, int n);
 int orc_dt_record(orc_domain *d, int capacity);
 const double *orc_dt_recorded(orc_domain *d);
 
+/* Decision tape, for finite differences along one branch of the cycle
+ * (compiled into build/liblulesh_oracle_tape.so; the other builds return
+ * -1).  orc_tape_record: the next ncycles cycles of orc_step store the
+ * outcome of every branch that changes a state value (limiter min/max,
+ * vdov and delv*delx switches, eosvmin/eosvmax, delvc > 0, emin, pmin,
+ * sound-speed floors) and the offset of every noise cut-off that fired
+ * (u_cut, p_cut, e_cut, q_cut, v_cut).  orc_tape_replay: the next cycles of
+ * d take src's recorded outcomes and add src's offsets where a cut-off
+ * fired -- a smooth map of d's state that equals the plain cycles bitwise
+ * on src's trajectory (src must outlive d's use).  orc_tape_stop: plain
+ * cycles again. */
+int orc_tape_record(orc_domain *d, int ncycles);
+int orc_tape_replay(orc_domain *d, const orc_domain *src);
+int orc_tape_stop(orc_domain *d);
+
 /* Rebuild the corner-per-node list from the current nodelist
  * (lulesh-init.cc:272-337).  Call after replacing nodelist. */
 void orc_rebuild_corner_list(orc_domain *d);

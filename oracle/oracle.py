@@ -19,6 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "build", "liblulesh_oracle.so")
 FAST_LIB = os.path.join(HERE, "build", "liblulesh_oracle_fast.so")
+TAPE_LIB = os.path.join(HERE, "build", "liblulesh_oracle_tape.so")
+TAPE_LD_LIB = os.path.join(HERE, "build", "liblulesh_oracle_tape_ld.so")
 REF_LIB = os.path.join(HERE, "_ref", "liblulesh_ref.so")
 REF_BIN = os.path.join(HERE, "_ref", "lulesh_ref")
 
@@ -30,12 +32,20 @@ SCALARS = ["time", "deltatime", "dtcourant", "dthydro", "cycle"]
 
 
 def build(ref: bool = True) -> None:
-    """Compile the restatement (and the reference build when its sources exist)."""
-    targets = ["port"] + (["ref"] if ref else [])
+    """Compile the restatement (parity, fast, tape and long double builds) and
+    the reference build when its sources exist."""
+    targets = ["port", "ld"] + (["ref"] if ref else [])
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
 
 _libs: dict[str, ctypes.CDLL] = {}
+
+
+def _view(ptr, n: int, dtype) -> np.ndarray:
+    """writable numpy view of n values of dtype at a ctypes pointer"""
+    addr = ctypes.cast(ptr, ctypes.c_void_p).value
+    buf = (ctypes.c_char * (n * np.dtype(dtype).itemsize)).from_address(addr)
+    return np.frombuffer(buf, dtype=dtype, count=n)
 
 
 def _load(path: str) -> ctypes.CDLL:
@@ -48,25 +58,30 @@ def _load(path: str) -> ctypes.CDLL:
     return lib
 
 
-def _port(lib_path: str = PORT_LIB) -> ctypes.CDLL:
+def _port(lib_path: str = PORT_LIB, real=ctypes.c_double) -> ctypes.CDLL:
+    """The restatement's entry points; real: the build's floating type."""
     lib = _load(lib_path)
+    R = ctypes.POINTER(real)
     lib.orc_create_ex.restype = ctypes.c_void_p
-    lib.orc_create_ex.argtypes = [ctypes.c_int] * 4 + [ctypes.c_double] * 2
+    lib.orc_create_ex.argtypes = [ctypes.c_int] * 4 + [real] * 2
     lib.orc_destroy.argtypes = [ctypes.c_void_p]
     lib.orc_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.orc_phase.argtypes = [ctypes.c_void_p, ctypes.c_int]
-    lib.orc_field_f64.restype = ctypes.POINTER(ctypes.c_double)
+    lib.orc_field_f64.restype = R
     lib.orc_field_f64.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t)]
     lib.orc_field_i32.restype = ctypes.POINTER(ctypes.c_int)
     lib.orc_field_i32.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t)]
-    lib.orc_get_scalar.restype = ctypes.c_double
+    lib.orc_get_scalar.restype = real
     lib.orc_get_scalar.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
-    lib.orc_set_scalar.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double]
+    lib.orc_set_scalar.argtypes = [ctypes.c_void_p, ctypes.c_char_p, real]
     lib.orc_region_rep.argtypes = [ctypes.c_void_p, ctypes.c_int]
-    lib.orc_dt_freeze.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    lib.orc_dt_freeze.argtypes = [ctypes.c_void_p, R, ctypes.c_int]
     lib.orc_dt_record.argtypes = [ctypes.c_void_p, ctypes.c_int]
-    lib.orc_dt_recorded.restype = ctypes.POINTER(ctypes.c_double)
+    lib.orc_dt_recorded.restype = R
     lib.orc_dt_recorded.argtypes = [ctypes.c_void_p]
+    lib.orc_tape_record.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.orc_tape_replay.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.orc_tape_stop.argtypes = [ctypes.c_void_p]
     return lib
 
 
@@ -74,8 +89,15 @@ class OracleDomain:
     """The C restatement: build the Sedov problem and advance it on the CPU."""
 
     def __init__(self, nx: int, numReg: int = 11, balance: int = 1, cost: int = 1,
-                 hgcoef: float = 3.0, einit_factor: float = 1.0, fast: bool = False):
-        self._lib = _port(FAST_LIB if fast else PORT_LIB)
+                 hgcoef: float = 3.0, einit_factor: float = 1.0, fast: bool = False,
+                 tape: bool = False, extended: bool = False):
+        """fast: the default-contraction build (timing); tape: the parity
+        build with the decision tape (tape_record / tape_replay); extended:
+        the tape build in long double (fields are np.longdouble)."""
+        self._real = ctypes.c_longdouble if extended else ctypes.c_double
+        self._dtype = np.longdouble if extended else np.float64
+        self._lib = _port(TAPE_LD_LIB if extended else TAPE_LIB if tape else
+                          FAST_LIB if fast else PORT_LIB, self._real)
         self._h = self._lib.orc_create_ex(nx, numReg, balance, cost, hgcoef, einit_factor)
         if not self._h:
             raise ValueError("invalid problem size")
@@ -103,7 +125,7 @@ class OracleDomain:
         n = ctypes.c_size_t()
         p = self._lib.orc_field_f64(self._h, name.encode(), ctypes.byref(n))
         if p:
-            return np.ctypeslib.as_array(p, shape=(n.value,))
+            return _view(p, n.value, self._dtype)
         p = self._lib.orc_field_i32(self._h, name.encode(), ctypes.byref(n))
         if p:
             return np.ctypeslib.as_array(p, shape=(n.value,))
@@ -120,14 +142,30 @@ class OracleDomain:
         return self._lib.orc_region_rep(self._h, r)
 
     def dt_freeze(self, dts) -> None:
-        a = np.ascontiguousarray(dts, dtype=np.float64)
-        self._lib.orc_dt_freeze(self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), a.size)
+        a = np.ascontiguousarray(dts, dtype=self._dtype)
+        self._lib.orc_dt_freeze(self._h, a.ctypes.data_as(ctypes.POINTER(self._real)), a.size)
 
     def dt_record(self, capacity: int) -> None:
         self._lib.orc_dt_record(self._h, capacity)
 
     def dt_recorded(self, n: int) -> np.ndarray:
-        return np.ctypeslib.as_array(self._lib.orc_dt_recorded(self._h), shape=(n,)).copy()
+        return _view(self._lib.orc_dt_recorded(self._h), n, self._dtype).copy()
+
+    def tape_record(self, ncycles: int) -> None:
+        """Record the branch outcomes of the next ncycles cycles."""
+        if self._lib.orc_tape_record(self._h, ncycles):
+            raise RuntimeError("decision tape unavailable (build with tape=True)")
+
+    def tape_replay(self, src: "OracleDomain") -> None:
+        """Replay src's recorded branches in this domain's next cycles; src
+        must stay alive while this domain steps."""
+        if self._lib.orc_tape_replay(self._h, src._h):
+            raise RuntimeError("no recorded tape in src, or a different mesh")
+        self._tape_src = src
+
+    def tape_stop(self) -> None:
+        self._lib.orc_tape_stop(self._h)
+        self._tape_src = None
 
     def state(self) -> dict:
         out = {f: self.field(f).copy() for f in NODE_FIELDS + ELEM_FIELDS}
@@ -142,6 +180,7 @@ def _ref() -> ctypes.CDLL:
     lib.ref_create.argtypes = [ctypes.c_int] * 4 + [ctypes.c_double] * 2
     lib.ref_destroy.argtypes = [ctypes.c_void_p]
     lib.ref_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.ref_step_frozen.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
     lib.ref_field_f64.restype = ctypes.POINTER(ctypes.c_double)
     lib.ref_field_f64.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t)]
     lib.ref_field_i32.restype = ctypes.POINTER(ctypes.c_int)
@@ -173,6 +212,12 @@ class RefDomain:
 
     def step(self, ncycles: int) -> int:
         return self._lib.ref_step(self._h, ncycles)
+
+    def step_frozen(self, dts) -> int:
+        """len(dts) cycles, cycle c advancing by dts[c]."""
+        a = np.ascontiguousarray(dts, dtype=np.float64)
+        return self._lib.ref_step_frozen(self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                         a.size)
 
     def field(self, name: str) -> np.ndarray:
         n = ctypes.c_size_t()

@@ -68,6 +68,21 @@ int ref_step(void *h, int ncycles)
     return d.cycle();
 }
 
+// The main loop with the time steps given: cycle c advances by dts[c]
+// instead of TimeIncrement's choice (the bookkeeping of lulesh.cc:218-221),
+// then LagrangeLeapFrog.
+int ref_step_frozen(void *h, const double *dts, int ncycles)
+{
+    Domain &d = *static_cast<Domain *>(h);
+    for (int c = 0; c < ncycles; ++c) {
+        d.deltatime() = dts[c];
+        d.time() += d.deltatime();
+        ++d.cycle();
+        LagrangeLeapFrog(d);
+    }
+    return d.cycle();
+}
+
 double *ref_field_f64(void *h, const char *name, size_t *n)
 {
     Domain &d = *static_cast<Domain *>(h);

@@ -10,6 +10,10 @@
 //        (prints per-check errors, then WORST; dump.bin receives nx, ncycles,
 //        the initial energy field, the frozen steps, the mask and the
 //        gradients, for comparing another implementation on the same inputs)
+// Environment: LG_FD_REL  relative step (default 1e-6)
+//              LG_FD_BRANCH=1  differences replay the forward run's branch
+//                 decisions (orc_tape_replay; needs the oracle compiled with
+//                 -DORC_TAPE) instead of re-deciding them
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -53,9 +57,15 @@ static orc_domain *fresh(const Run &r, const vector<double> &e0, double hg)
     return d;
 }
 
+static orc_domain *g_tape = nullptr;  // recorded run the differences replay
+
 static double objective(const Run &r, const vector<double> &e0, double hg)
 {
     orc_domain *d = fresh(r, e0, hg);
+    if (g_tape && orc_tape_replay(d, g_tape) != 0) {
+        fprintf(stderr, "no decision tape (oracle built without -DORC_TAPE)\n");
+        exit(2);
+    }
     if (orc_step(d, r.ncyc) != 0) {
         fprintf(stderr, "forward failed\n");
         exit(2);
@@ -118,6 +128,14 @@ int main(int argc, char **argv)
                             "delv_xi", "delv_eta", "delv_zeta"};
     const size_t snapD = 6 * (size_t)N + 5 * (size_t)E;
     vector<double> snaps((r.ncyc + 1) * snapD), temps(r.ncyc * 8 * (size_t)E);
+    const bool branch = getenv("LG_FD_BRANCH") && atoi(getenv("LG_FD_BRANCH"));
+    if (branch) {
+        if (orc_tape_record(d, r.ncyc) != 0) {
+            fprintf(stderr, "no decision tape (oracle built without -DORC_TAPE)\n");
+            return 2;
+        }
+        g_tape = d;
+    }
     auto save = [&](int c) {
         double *b = &snaps[c * snapD];
         for (int i = 0; i < 6; ++i) {

@@ -4,10 +4,10 @@ J = total internal energy sum(e * volo) of the elements whose centroid lies
 within r = 0.5 of the origin after the last cycle; the time-step sequence is
 frozen from the forward run of the noisy initial field (tests/adjoint_case.py).
 Gradients with respect to the initial energy field (16 seeded directions) and
-hgcoef are compared with central differences of the plain GPU path at
-relative step 1e-6, and -- where the fixture exists -- with central
-differences of the reference CPU build computed the same way
-(tests/golden/make_golden.py).  Bar: 1e-6 relative.
+hgcoef are compared with central differences of the plain GPU path and, at
+the full size, with central differences of the oracle replaying the base
+run's branch decisions and of the reference CPU build
+(tests/golden/make_adjoint_fd.py).  Bar: 1e-6 relative.
 """
 import json
 import os
@@ -96,13 +96,33 @@ def test_autograd_binding(native_lib):
 
 
 def test_adjoint_s48_200_cycles(native_lib, capsys):
-    """The full study: s=48, 200 cycles, checkpoint every 20.  Over 200
-    cycles the noisy field drives delvc through zero in elements whose
-    monotonic-Q terms are nonzero, so J jumps (lulesh.cc:2079-2081,
-    2122-2124) many times within one finite-difference step; the plain
-    central differences are printed, and the adjoint is checked for cost
-    and for agreeing with the forward objective."""
-    pr, e_noisy, idx, e0 = _problem(case.NX, case.NCYCLES, case.CKPT)
+    """The full study: s=48, 200 cycles, checkpoint every 20, on the time
+    steps and mask of the fixture's oracle run.
+
+    Over 200 cycles the noisy field drives delvc through zero in elements
+    whose monotonic-Q terms are nonzero, so J itself jumps (lulesh.cc:
+    2079-2081, 2122-2124) many times within one finite-difference step, in
+    the reference build as in this path; plain central differences of the
+    two agree with each other, not with any derivative.  The adjoint is
+    checked against central differences of the oracle replaying the branch
+    decisions of the base run (orc_tape_replay), which is smooth there;
+    elements crossing zero energy put square roots of near-zero arguments
+    on that branch, so its differences converge (as h^2) only below relative
+    step 1e-8, where double-precision round-off of J (~2e-13) already costs
+    1e-6..1e-5 of the smaller derivatives.  The check of record is the
+    replay in long double (2,000x less round-off) at steps 1e-9 and 1e-10,
+    Richardson-extrapolated."""
+    if not os.path.exists(GOLDEN):
+        pytest.skip("adjoint fixture not generated (tests/golden/make_adjoint_fd.py)")
+    g = json.load(open(GOLDEN))
+    from lulesh_gb300.autograd import TerminalEnergyProblem
+    import lulesh_gb300 as lg
+    e_setup = lg.Domain(case.NX, case.NREG, device=-1).field("e")
+    e_noisy, idx = case.initial_energy(e_setup, case.NX)
+    mask = np.zeros(case.NX ** 3, bool)
+    mask[g["mask_idx"]] = True
+    pr = TerminalEnergyProblem(case.NX, case.NREG, case.NCYCLES, case.CKPT, e_base=e_noisy,
+                               dts=np.array(g["dts"]), mask=mask)
     Jf = pr.objective(e_noisy, pr.hg_base)
     t_fwd = t_adj = float("inf")
     for _ in range(3):
@@ -112,15 +132,56 @@ def test_adjoint_s48_200_cycles(native_lib, capsys):
         t0 = time.perf_counter()
         J, ge, gh = pr.value_and_grad(e_noisy, pr.hg_base)
         t_adj = min(t_adj, time.perf_counter() - t0)
-    errs6 = _fd_checks(pr, e_noisy, idx, e0, case.NDIR, rel=1e-6)[3]
+    dirs = case.directions(idx, e_noisy)
+    ad = [float(ge @ d) for d in dirs] + [gh * case.REL_STEP * pr.hg_base]
+
+    def along(tab, rel):
+        """a fixture table as derivatives along the step-1e-6 directions"""
+        k = rel / case.REL_STEP
+        return [None if f is None else f / k for f in tab["e0"]] + [
+            None if tab["hgcoef"] is None else tab["hgcoef"] * case.REL_STEP * pr.hg_base]
+
+    def errs(fd):
+        return [None if f is None else abs(a - f) / abs(f) for a, f in zip(ad, fd)]
+
+    steps = {r: along(t, float(r)) for r, t in g["branch_fd"].items()}
+    ext = {r: along(t, float(r)) for r, t in g["branch_fd_extended"].items()}
+
+    def richardson(coarse, fine):
+        # central differences at h and h/10 with an O(h^2) error:
+        # D = D(h/10) + (D(h/10) - D(h)) / 99
+        return [None if a is None or b is None else b + (b - a) / 99 for a, b in zip(coarse, fine)]
+
+    rich = richardson(steps["1e-08"], steps["1e-09"])
+    rich_ext = richardson(ext["1e-09"], ext["1e-10"])
+    plain_ref = errs(along(g["plain_fd_ref"]["1e-06"], 1e-6))
+    # this path's own plain central differences at relative step 1e-6
+    fd_gpu = [(pr.objective(e_noisy + d, pr.hg_base) - pr.objective(e_noisy - d, pr.hg_base)) / 2
+              for d in dirs]
+    fd_ref = g["plain_fd_ref"]["1e-06"]["e0"]
+    scale = max(abs(f) for f in fd_ref)
+    plain_vs_ref = max(abs(a - b) for a, b in zip(fd_gpu, fd_ref)) / scale
+    fmt = lambda v: " ".join("  -    " if x is None else f"{x:.1e}" for x in v)  # noqa: E731
     with capsys.disabled():
-        print(f"\nadjoint s=48/200: J={J:.10e} dJ/dhg={gh:.6e} adjoint/forward time "
-              f"{t_adj / t_fwd:.2f}\n  plain FD rel err at step 1e-6: "
-              + " ".join(f"{e:.1e}" for e in errs6))
+        print(f"\nadjoint s=48/200: J={J:.12e} (oracle {g['J_oracle']:.12e}, reference "
+              f"{g['J_ref']:.12e}) dJ/dhg={gh:.6e} adjoint/forward time {t_adj / t_fwd:.2f}")
+        print("  relative error of the adjoint's 16 directional derivatives and dJ/dhgcoef")
+        for r, fd in steps.items():
+            print(f"  vs branch-replay FD, step {r}: " + fmt(errs(fd)))
+        print("  vs branch-replay FD, Richardson 1e-8/1e-9: " + fmt(errs(rich)))
+        for r, fd in ext.items():
+            print(f"  vs extended-precision branch-replay FD, step {r}: " + fmt(errs(fd)))
+        print("  vs extended-precision branch-replay FD, Richardson 1e-9/1e-10: "
+              + fmt(errs(rich_ext)))
+        print("  vs reference plain FD, step 1e-6: " + fmt(plain_ref))
+        print(f"  plain FD of this path vs the reference build's: {plain_vs_ref:.1e} "
+              "(of the largest)")
     assert abs(J / Jf - 1) <= 1e-12
+    assert abs(J / g["J_ref"] - 1) <= 1e-10 and abs(J / g["J_oracle"] - 1) <= 1e-10
     assert t_adj <= 4 * t_fwd
-    # hgcoef moves every element smoothly: plain differences resolve it
-    assert errs6[-1] <= TOL
-    if os.path.exists(GOLDEN):
-        g = json.load(open(GOLDEN))
-        assert abs(J / g["J"] - 1) <= 1e-9
+    # every directional derivative agrees with the extended-precision replay
+    # differences to 1e-6
+    checked = errs(rich_ext)
+    assert None not in checked and max(checked) <= TOL, checked
+    # the forward path differentiates like the reference build
+    assert plain_vs_ref <= 1e-6

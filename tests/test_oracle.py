@@ -142,3 +142,88 @@ print("ok")
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
                        env=dict(os.environ, OMP_NUM_THREADS="4"))
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr
+
+
+def _noisy_case(lib_kw, nx=10, ncyc=30):
+    """the adjoint study's kind of input on a small mesh: the set-up field
+    with N(0, 1e-3 e0) noise near the origin, its forward run's time steps"""
+    from oracle.oracle import OracleDomain
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import adjoint_case as case
+    s0 = OracleDomain(nx, 11)
+    e, _ = case.initial_energy(s0.field("e").copy(), nx, 200)
+    b = OracleDomain(nx, 11)
+    b.field("e")[:] = e
+    b.dt_record(ncyc)
+    assert b.step(ncyc) == 0
+    return e, b.dt_recorded(ncyc), b
+
+
+def test_tape_record_and_replay_reproduce_the_plain_cycle(oracle_built):
+    """The decision tape changes nothing at the recorded point: the tape
+    build recording, and a second domain replaying the recording, both give
+    the parity build's fields bit for bit."""
+    from oracle.oracle import OracleDomain, NODE_FIELDS, ELEM_FIELDS
+    e, dts, plain = _noisy_case({})
+    rec = OracleDomain(10, 11, tape=True)
+    rec.field("e")[:] = e
+    rec.dt_freeze(dts)
+    rec.tape_record(len(dts))
+    assert rec.step(len(dts)) == 0
+    rep = OracleDomain(10, 11, tape=True)
+    rep.field("e")[:] = e
+    rep.dt_freeze(dts)
+    rep.tape_replay(rec)
+    assert rep.step(len(dts)) == 0
+    for f in NODE_FIELDS + ELEM_FIELDS:
+        assert np.array_equal(plain.field(f), rec.field(f)), f
+        assert np.array_equal(plain.field(f), rep.field(f)), f
+    with pytest.raises(RuntimeError):
+        OracleDomain(10, 11).tape_record(5)        # the parity build has no tape
+
+
+def test_tape_replay_holds_the_recorded_branches(oracle_built):
+    """Away from the recorded point a replay keeps the recorded decisions.
+    A cold element of the set-up field (e = 0, so p = 0: no pmin clamp) is
+    given e = -1: the plain cycle clamps its pressure to pmin = 0, the
+    replay keeps the recorded branch p = bvc * e < 0."""
+    from oracle.oracle import OracleDomain
+    k = 10 ** 3 - 1                                  # far corner, cold for many cycles
+    rec = OracleDomain(10, 11, tape=True)
+    e = rec.field("e").copy()
+    rec.tape_record(1)
+    assert rec.step(1) == 0
+    dts = [rec.scalar("deltatime")]
+    runs = {}
+    for mode in ("plain", "replay"):
+        d = OracleDomain(10, 11, tape=True)
+        d.field("e")[:] = e
+        d.field("e")[k] = -1.0
+        d.dt_freeze(dts)
+        if mode == "replay":
+            d.tape_replay(rec)
+        assert d.step(1) == 0
+        runs[mode] = d.field("p")[k]
+    assert runs["plain"] == 0.0
+    assert runs["replay"] < 0.0
+
+
+def test_extended_precision_build(oracle_built):
+    """The long double tape build: the same problem to rounding of double
+    precision, and its own recording replays bit for bit."""
+    from oracle.oracle import OracleDomain
+    e, dts, plain = _noisy_case({}, ncyc=20)
+    rec = OracleDomain(10, 11, extended=True)
+    assert rec.field("e").dtype == np.longdouble
+    rec.field("e")[:] = e
+    rec.dt_freeze(dts)
+    rec.tape_record(len(dts))
+    assert rec.step(len(dts)) == 0
+    rep = OracleDomain(10, 11, extended=True)
+    rep.field("e")[:] = e
+    rep.dt_freeze(dts)
+    rep.tape_replay(rec)
+    assert rep.step(len(dts)) == 0
+    assert np.array_equal(rec.field("e"), rep.field("e"))
+    ef, el = plain.field("e"), rec.field("e").astype(np.float64)
+    assert np.max(np.abs(el - ef)) <= 1e-12 * np.max(np.abs(ef))
