@@ -5,12 +5,14 @@ One "step" is one cycle of the reference main loop (TimeIncrement +
 LagrangeLeapFrog, lulesh.cc:2745-2757) over the whole mesh.  The default
 workload is the reference's built-in Sedov problem at s=150 (3,375,000
 elements, 11 regions, balance 1, cost 1), 500 cycles from the initial state,
-FP64.  The state (~2 GB) is larger than the 129 MB L2, so no flush is needed
-between cycles.
+FP64 with fused multiply-add (within 1e-10 of the reference's OpenMP build on
+every field after the 500 cycles; `--precision fp64` runs without
+contraction).  The state (~2 GB) is larger than the 129 MB L2, so no flush is
+needed between cycles.
 
     python bench.py [--steps 500] [--warmup 5] [--gpus N] [--impl gb300|reference]
                     [--nx 150] [--regions 11] [--balance 1] [--cost 1]
-                    [--precision fp64|fp64-fma|mixed]
+                    [--precision fp64-fma|fp64|mixed] [--ensemble N] [--err-vs-fp64]
 
 Prints one JSON line.  `value` is the device-timed rate (CUDA events on the
 handle's stream around exactly K cycles, the state resident in HBM);
@@ -61,10 +63,15 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 
 
 # FP64 thread-instructions (DADD + DMUL + DFMA) per element per launch,
-# from an ncu capture of each kernel (profiles/); None where not measured.
+# from an ncu capture of each kernel of the strict and the FMA build at
+# s=100 (profiles/leapfrog_fp64_s100_ncu.md; k_nodes: per node, stored per
+# element at s=100's N/E; k_material: the s=100 region mix); absent where
+# not measured.
 FP64_INST_PER_ELEM = {
-    "fp64": {},
-    "fp64-fma": {},
+    "fp64": {"k_forces": 1363, "k_kinematics": 728, "k_material": 770,
+             "k_nodes": 113 * 1030301 / 1000000},
+    "fp64-fma": {"k_forces": 955, "k_kinematics": 606, "k_material": 729,
+                 "k_nodes": 109.6 * 1030301 / 1000000},
 }
 
 
@@ -230,7 +237,7 @@ def d_device(d) -> int:
 
 
 def run_ensemble(a):
-    """The batched ensemble (BASELINE config 4) against the plain path run
+    """The batched ensemble (64 sampled Sedov problems) against the plain path run
     member by member, same members, same precision, same cycles."""
     dist, ws, rank, local = _dist()
     import numpy as np
@@ -457,7 +464,11 @@ def main():
     p.add_argument("--regions", type=int, default=11)
     p.add_argument("--balance", type=int, default=1)
     p.add_argument("--cost", type=int, default=1)
-    p.add_argument("--precision", default="fp64", choices=["fp64", "fp64-fma", "mixed"])
+    p.add_argument("--precision", default="fp64-fma", choices=["fp64", "fp64-fma", "mixed"],
+                   help="fp64-fma (default): FP64 with fused multiply-add, within 1e-10 of "
+                        "the reference at s=150/500 cycles; fp64: no contraction (the "
+                        "reference's arithmetic operation for operation); mixed: FP32 "
+                        "forces/kinematics/Q with FP64 state and EOS")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--ensemble", type=int, default=0,
                    help="batched ensemble of this many sampled problems instead of one problem")
