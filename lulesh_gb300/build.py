@@ -39,6 +39,7 @@ CUDA_UNITS = [
     ("lg_adjoint.cu", ["--fmad=true"]),
     ("lg_peak.cu", ["--fmad=true"]),
     ("lg_noalloc.cu", ["--fmad=false"]),
+    ("lg_setup.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["lg_problem.cc"]
 
@@ -106,8 +107,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             if verbose:
                 print(" ".join(cmd), file=sys.stderr)
         list(ex.map(_run, steps))
-    if _stale(LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs)
+    exports = os.path.join(CSRC, "exports.map")
+    if _stale(LIB, objs + [exports]):
+        # only the C ABI (lg_*) is exported; internal C++ symbols stay local
+        _run([nvcc] + ARCH + ["-shared", "-Xlinker", "--version-script=" + exports, "-o", LIB]
+             + objs)
     if _stale(CLI, [cli_obj, LIB]):
         _run(["g++", "-o", CLI, cli_obj, "-L" + LIBDIR, "-llulesh_gb300",
               "-Wl,-rpath,$ORIGIN/../lib"])

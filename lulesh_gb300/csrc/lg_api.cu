@@ -61,7 +61,12 @@ int record_error(int code, const char *msg) { return set_error(code, "%s", msg);
 
 struct lg_domain {
     lg_opts opts{};
-    lg::Problem prob;  // host mirror: integer fields and the initial state
+    // host mirror: sizes, constants, time state and regions always; the
+    // initial double fields when mirror_state (host-only handles), the
+    // integer topology when mirror_topo (host-only handles, or downloaded on
+    // first use from the device that built it)
+    lg::Problem prob;
+    bool mirror_state = false, mirror_topo = false;
     lg::DevState ds{};
     const lg::KernelSet *ks = nullptr;
     void *arena = nullptr;
@@ -92,6 +97,8 @@ struct AdjointIO {
     const std::vector<int> *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *elemBC;
 };
 int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg);
+cudaError_t device_setup(const DevState &s, int nx, double einit, bool topology,
+                         cudaStream_t stream);
 }  // namespace lg
 
 namespace {
@@ -140,18 +147,12 @@ int upload_inv_mass(lg_domain *d, const double *m, size_t n)
     return upload(d, d->ds.invMass, inv);
 }
 
-// Kernel-side layouts derived from the integer fields (see lg_device.h).
-int upload_topology(lg_domain *d)
+// regNumList and the region-ordered element permutation with each
+// position's EOS repetition count, from the host region sets.
+int upload_regions(lg_domain *d)
 {
     const lg::Problem &p = d->prob;
-    const int E = p.numElem, N = p.numNode;
-    std::vector<int> nlT(8 * (size_t)E);
-    for (int e = 0; e < E; ++e)
-        for (int j = 0; j < 8; ++j) nlT[(size_t)j * E + e] = p.nodelist[8 * (size_t)e + j];
-    std::vector<uint8_t> symm(N, 0);
-    for (int n : p.symmX) symm[n] |= 1;
-    for (int n : p.symmY) symm[n] |= 2;
-    for (int n : p.symmZ) symm[n] |= 4;
+    const int E = p.numElem;
     std::vector<int> perm, rep;
     perm.reserve(E);
     rep.reserve(E);
@@ -163,6 +164,27 @@ int upload_topology(lg_domain *d)
         }
     }
     if ((int)perm.size() != E) return set_error(LG_ERR_INVALID, "region sets do not cover all elements");
+    int st;
+    if ((st = upload(d, d->ds.regNumList, p.regNumList))) return st;
+    if ((st = upload(d, d->ds.regPerm, perm))) return st;
+    if ((st = upload(d, d->ds.regRep, rep))) return st;
+    LG_CUDA(cudaStreamSynchronize(d->stream));
+    return LG_OK;
+}
+
+// Kernel-side layouts derived from the host mirror's integer fields (see
+// lg_device.h).
+int upload_topology(lg_domain *d)
+{
+    const lg::Problem &p = d->prob;
+    const int E = p.numElem, N = p.numNode;
+    std::vector<int> nlT(8 * (size_t)E);
+    for (int e = 0; e < E; ++e)
+        for (int j = 0; j < 8; ++j) nlT[(size_t)j * E + e] = p.nodelist[8 * (size_t)e + j];
+    std::vector<uint8_t> symm(N, 0);
+    for (int n : p.symmX) symm[n] |= 1;
+    for (int n : p.symmY) symm[n] |= 2;
+    for (int n : p.symmZ) symm[n] |= 4;
     int st;
     if ((st = upload(d, d->ds.nodelist, p.nodelist))) return st;
     if ((st = upload(d, d->ds.nodelistT, nlT))) return st;
@@ -176,10 +198,50 @@ int upload_topology(lg_domain *d)
     if ((st = upload(d, d->ds.lzetam, p.lzetam))) return st;
     if ((st = upload(d, d->ds.lzetap, p.lzetap))) return st;
     if ((st = upload(d, d->ds.elemBC, p.elemBC))) return st;
-    if ((st = upload(d, d->ds.regNumList, p.regNumList))) return st;
-    if ((st = upload(d, d->ds.regPerm, perm))) return st;
-    if ((st = upload(d, d->ds.regRep, rep))) return st;
+    return upload_regions(d);
+}
+
+template <typename T>
+int download(lg_domain *d, std::vector<T> &dst, const T *src, size_t n)
+{
+    dst.resize(n);
+    if (n) LG_CUDA(cudaMemcpyAsync(dst.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost,
+                                   d->stream));
+    return LG_OK;
+}
+
+// The integer topology in the host mirror: downloaded from the device that
+// built it, once (afterwards the mirror is the master copy: lg_set_field
+// edits it and uploads it).
+int ensure_topology_mirror(lg_domain *d)
+{
+    if (d->host_only || d->mirror_topo) return LG_OK;
+    lg::Problem &p = d->prob;
+    const lg::DevState &s = d->ds;
+    const size_t E = p.numElem, N = p.numNode;
+    int st;
+    if ((st = download(d, p.nodelist, s.nodelist, 8 * E))) return st;
+    if ((st = download(d, p.lxim, s.lxim, E))) return st;
+    if ((st = download(d, p.lxip, s.lxip, E))) return st;
+    if ((st = download(d, p.letam, s.letam, E))) return st;
+    if ((st = download(d, p.letap, s.letap, E))) return st;
+    if ((st = download(d, p.lzetam, s.lzetam, E))) return st;
+    if ((st = download(d, p.lzetap, s.lzetap, E))) return st;
+    if ((st = download(d, p.elemBC, s.elemBC, E))) return st;
+    if ((st = download(d, p.nodeElemStart, s.nodeElemStart, N + 1))) return st;
+    if ((st = download(d, p.nodeElemCornerList, s.nodeElemCornerList, 8 * E))) return st;
+    std::vector<uint8_t> symm;
+    if ((st = download(d, symm, s.symm, N))) return st;
     LG_CUDA(cudaStreamSynchronize(d->stream));
+    p.symmX.clear();
+    p.symmY.clear();
+    p.symmZ.clear();
+    for (size_t n = 0; n < N; ++n) {  // ascending node order, as SetupSymmetryPlanes lists them
+        if (symm[n] & 1) p.symmX.push_back((int)n);
+        if (symm[n] & 2) p.symmY.push_back((int)n);
+        if (symm[n] & 4) p.symmZ.push_back((int)n);
+    }
+    d->mirror_topo = true;
     return LG_OK;
 }
 
@@ -308,26 +370,38 @@ int enqueue_cycles(lg_domain *d, int ncycles)
     return LG_OK;
 }
 
-// Upload the state built by set-up (fields, topology, time-step state).
-int upload_initial_state(lg_domain *d)
+// Put the set-up state on the device: the initial fields (uploaded from the
+// host mirror where it holds them, else rebuilt by the set-up kernels), the
+// topology where the host mirror holds it (at creation without a mirror the
+// set-up kernels build it), and the time-step state.
+int upload_initial_state(lg_domain *d, bool creating)
 {
     lg::Problem &p = d->prob;
     int st;
-    double *fld;
-    size_t cnt;
-    std::vector<double> *hostf[26] = {&p.x, &p.y, &p.z, &p.xd, &p.yd, &p.zd, &p.xdd, &p.ydd,
-                                      &p.zdd, &p.fx, &p.fy, &p.fz, &p.nodalMass, &p.e, &p.p,
-                                      &p.q, &p.ql, &p.qq, &p.v, &p.volo, &p.vnew, &p.delv,
-                                      &p.vdov, &p.arealg, &p.ss, &p.elemMass};
-    const char *names[26] = {"x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy",
-                             "fz", "nodalMass", "e", "p", "q", "ql", "qq", "v", "volo", "vnew",
-                             "delv", "vdov", "arealg", "ss", "elemMass"};
-    for (int i = 0; i < 26; ++i) {
-        find_f64(d, names[i], &fld, &cnt);
-        if ((st = upload(d, fld, *hostf[i]))) return st;
+    if (d->mirror_state) {
+        double *fld;
+        size_t cnt;
+        std::vector<double> *hostf[26] = {&p.x, &p.y, &p.z, &p.xd, &p.yd, &p.zd, &p.xdd, &p.ydd,
+                                          &p.zdd, &p.fx, &p.fy, &p.fz, &p.nodalMass, &p.e, &p.p,
+                                          &p.q, &p.ql, &p.qq, &p.v, &p.volo, &p.vnew, &p.delv,
+                                          &p.vdov, &p.arealg, &p.ss, &p.elemMass};
+        const char *names[26] = {"x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy",
+                                 "fz", "nodalMass", "e", "p", "q", "ql", "qq", "v", "volo", "vnew",
+                                 "delv", "vdov", "arealg", "ss", "elemMass"};
+        for (int i = 0; i < 26; ++i) {
+            find_f64(d, names[i], &fld, &cnt);
+            if ((st = upload(d, fld, *hostf[i]))) return st;
+        }
+        if ((st = upload_inv_mass(d, p.nodalMass.data(), p.nodalMass.size()))) return st;
+    } else {
+        LG_CUDA(lg::device_setup(d->ds, p.nx, lg::sedov_einit(p.nx, d->opts.einit_factor),
+                                 creating && !d->mirror_topo, d->stream));
     }
-    if ((st = upload_topology(d))) return st;
-    if ((st = upload_inv_mass(d, p.nodalMass.data(), p.nodalMass.size()))) return st;
+    if (d->mirror_topo) {
+        if ((st = upload_topology(d))) return st;
+    } else if (creating) {
+        if ((st = upload_regions(d))) return st;
+    }
 
     lg::Ctl &c = *d->h_ctl;
     memset(&c, 0, sizeof(c));
@@ -395,8 +469,16 @@ int lg_create(const lg_opts *opts, lg_domain **out)
         delete d;
         return st;
     }
-    d->prob = lg::build_sedov(opts->nx, opts->numReg, opts->balance, opts->cost, opts->hgcoef,
-                              opts->einit_factor);
+    if (d->host_only) {
+        d->prob = lg::build_sedov(opts->nx, opts->numReg, opts->balance, opts->cost,
+                                  opts->hgcoef, opts->einit_factor);
+        d->mirror_state = d->mirror_topo = true;
+    } else {
+        // sizes, constants, time state and regions on the host; the mesh and
+        // the fields are built on the device (lg_setup.cu)
+        d->prob = lg::build_sedov_scalars(opts->nx, opts->numReg, opts->balance, opts->cost,
+                                          opts->hgcoef, opts->einit_factor);
+    }
     lg::Problem &p = d->prob;
     if (d->host_only) {
         d->ds.E = p.numElem;
@@ -468,7 +550,7 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     if (cudaMemsetAsync(d->arena, 0, L.total, d->stream) != cudaSuccess)
         return fail(set_error(LG_ERR_CUDA, "cudaMemset failed"));
 
-    if ((st = upload_initial_state(d))) return fail(st);
+    if ((st = upload_initial_state(d, true))) return fail(st);
     *out = d;
     return LG_OK;
 }
@@ -479,7 +561,7 @@ int lg_reset(lg_domain *d)
     int st;
     if ((st = ensure_device(d))) return st;
     LG_CUDA(cudaStreamSynchronize(d->stream));
-    return upload_initial_state(d);
+    return upload_initial_state(d, false);
 }
 
 void lg_destroy(lg_domain *d)
@@ -600,6 +682,8 @@ int lg_field_info(lg_domain *d, const char *name, size_t *count, int *dtype)
         if (dtype) *dtype = LG_F64;
         return LG_OK;
     }
+    int st;
+    if ((st = ensure_topology_mirror(d))) return st;
     if (std::vector<int> *v = find_i32(d, name)) {
         if (count) *count = v->size();
         if (dtype) *dtype = LG_I32;
@@ -633,6 +717,7 @@ int lg_get_field(lg_domain *d, const char *name, void *dst, size_t n)
         LG_CUDA(cudaStreamSynchronize(d->stream));
         return LG_OK;
     }
+    if ((st = ensure_topology_mirror(d))) return st;
     if (std::vector<int> *v = find_i32(d, name)) {
         if (n != v->size())
             return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, v->size(), n);
@@ -658,6 +743,7 @@ int lg_set_field(lg_domain *d, const char *name, const void *src, size_t n)
         LG_CUDA(cudaStreamSynchronize(d->stream));
         return LG_OK;
     }
+    if ((st = ensure_topology_mirror(d))) return st;
     std::vector<int> *v = find_i32(d, name);
     if (!v) return set_error(LG_ERR_INVALID, "unknown field '%s'", name);
     if (n != v->size())
@@ -876,6 +962,7 @@ int lg_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask,
         return set_error(LG_ERR_STATE, "lg_adjoint needs frozen time steps for cycles %d..%d "
                                        "(lg_dt_freeze)", c0, c0 + ncycles - 1);
     drop_graphs(d);  // the adjoint launches its own cycles
+    if ((st = ensure_topology_mirror(d))) return st;
     const lg::Problem &p = d->prob;
     lg::AdjointIO io{&d->ds, d->ks, d->stream, d->h_ctl, d->h_dtfrozen.data() + c0, ncycles,
                      ckpt_k, mask, d->ds.prm.hgcoef, &p.lxim, &p.lxip, &p.letam, &p.letap,

@@ -288,12 +288,39 @@ Problem build_sedov(int nx, int numReg, int balance, int cost, double hgcoef,
     }
 
     // deposited energy and analytic first step, lulesh-init.cc:183-192
+    const double einit = sedov_einit(nx, einit_factor);
+    p.e[0] = einit;
+    p.t.deltatime = (.5 * std::cbrt(p.volo[0])) / std::sqrt(2.0 * einit);
+    return p;
+}
+
+double sedov_einit(int nx, double einit_factor)
+{
     const double ebase = 3.948746e+7;
     const double scale = (nx * 1) / 45.0;
     double einit = ebase * scale * scale * scale;
-    einit = einit * einit_factor;
-    p.e[0] = einit;
-    p.t.deltatime = (.5 * std::cbrt(p.volo[0])) / std::sqrt(2.0 * einit);
+    return einit * einit_factor;
+}
+
+Problem build_sedov_scalars(int nx, int numReg, int balance, int cost, double hgcoef,
+                            double einit_factor)
+{
+    Problem p;
+    p.nx = nx;
+    p.balance = balance;
+    p.cost = cost;
+    p.k.hgcoef = hgcoef;
+    p.numElem = nx * nx * nx;
+    p.numNode = (nx + 1) * (nx + 1) * (nx + 1);
+    draw_regions(p, numReg, balance);
+    // element 0's corners at the BuildMesh coordinates 0 and 1.125 / nx
+    const double h = 1.125 * double(1) / double(nx);
+    const double x0[8] = {0.0, h, h, 0.0, 0.0, h, h, 0.0};
+    const double y0[8] = {0.0, 0.0, h, h, 0.0, 0.0, h, h};
+    const double z0[8] = {0.0, 0.0, 0.0, 0.0, h, h, h, h};
+    const double volo0 = elem_volume_host(x0, y0, z0);
+    const double einit = sedov_einit(nx, einit_factor);
+    p.t.deltatime = (.5 * std::cbrt(volo0)) / std::sqrt(2.0 * einit);
     return p;
 }
 

@@ -68,6 +68,17 @@ class GlibcRand {
 Problem build_sedov(int nx, int numReg, int balance, int cost, double hgcoef,
                     double einit_factor);
 
+// The part of build_sedov that stays on the host when the mesh is built on
+// the device (lg_setup.cu): sizes, constants, the time-step state (the first
+// step from the analytic volume of element 0) and the region draw, which
+// follows the reference's sequential random stream.  The mesh and field
+// vectors stay empty.
+Problem build_sedov_scalars(int nx, int numReg, int balance, int cost, double hgcoef,
+                            double einit_factor);
+
+// Deposited origin energy, lulesh-init.cc:183-189.
+double sedov_einit(int nx, double einit_factor);
+
 // SetupThreadSupportStructures (lulesh-init.cc:272-337) from p.nodelist.
 void build_corner_list(Problem &p);
 
