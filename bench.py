@@ -75,6 +75,20 @@ FP64_INST_PER_ELEM = {
 }
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element per
+# launch (k_nodes: per node), from one ncu capture of each kernel on a smaller
+# mesh of the same problem, scaled to the benchmarked mesh by the units it
+# processes: s=100 for the FP64 builds, s=96 r16 b2 c4 for the mixed one
+# (profiles/).  Well above the algorithmic bytes: the per-corner force
+# scratch (k_forces writes, k_nodes reads) and the region-order gathers of
+# k_material.
+TRAFFIC_PER_UNIT = {
+    "fp64": {"k_forces": 456.3, "k_nodes": 540.0, "k_kinematics": 140.1, "k_material": 224.3},
+    "fp64-fma": {"k_forces": 456.1, "k_nodes": 553.5, "k_kinematics": 138.9, "k_material": 220.1},
+    "mixed": {"k_forces": 264.7, "k_nodes": 338.2, "k_kinematics": 120.8, "k_material": 174.4},
+}
+
+
 def _peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -396,8 +410,12 @@ def run_gpu(a):
     peaks = _peaks()
     ab = alg_bytes_per_elem(dom, N / E) * E
     achieved = ab / (avg_ms * 1e-3) / 1e9
+    per_unit = TRAFFIC_PER_UNIT.get(a.precision, {}).get(dom)
+    traffic = None if per_unit is None else per_unit * (N if dom == "k_nodes" else E)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": dom,
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "traffic_source": "ncu DRAM bytes per unit on a smaller mesh, scaled"
+                if traffic else None, "kernel": dom,
                 "peak_source": peaks["src"], "alg_bytes_per_launch": ab,
                 "kernel_ms_per_launch": avg_ms,
                 "kernel_share": {k: v / total for k, v in prof.items()}}
