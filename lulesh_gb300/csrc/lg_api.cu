@@ -98,7 +98,8 @@ struct AdjointIO {
 };
 int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg);
 cudaError_t device_setup(const DevState &s, int nx, double einit, bool topology,
-                         cudaStream_t stream);
+                         cudaStream_t stream, int eoff = 0, int noff = 0, long long tstride = 0,
+                         int pid = 0);
 }  // namespace lg
 
 namespace {

@@ -25,6 +25,8 @@
 
 namespace lg {
 int record_error(int code, const char *msg);
+cudaError_t device_setup(const DevState &s, int nx, double einit, bool topology,
+                         cudaStream_t stream, int eoff, int noff, long long tstride, int pid);
 }
 
 namespace {
@@ -194,25 +196,43 @@ const char *kFields[26] = {"x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd",
                            "fy", "fz", "nodalMass", "e", "p", "q", "ql", "qq", "v", "volo",
                            "vnew", "delv", "vdov", "arealg", "ss", "elemMass"};
 
-// upload every problem's set-up state (fields, control blocks, slots)
-int upload_state(lg_ensemble *en)
+// member i's view of the concatenated arrays: every pointer moved to its
+// first element or node, its own sizes
+lg::DevState member_view(const lg_ensemble *en, int i)
 {
-    int st;
-    for (const char *f : kFields) {
-        bool node = false;
-        std::vector<double> all;
-        all.reserve(host_f64(en->prob[0], f, &node) && node ? en->N : en->E);
-        for (auto &p : en->prob) {
-            const std::vector<double> *v = host_f64(p, f, &node);
-            all.insert(all.end(), v->begin(), v->end());
-        }
-        if ((st = put(en, dev_f64(en->ds, f), all))) return st;
+    lg::DevState v = en->ds;
+    const long long eo = en->eoff[i], no = en->noff[i];
+    v.E = en->prob[i].numElem;
+    v.N = en->prob[i].numNode;
+    double **nodef[14] = {&v.x, &v.y, &v.z, &v.xd, &v.yd, &v.zd, &v.xdd, &v.ydd, &v.zdd,
+                          &v.fx, &v.fy, &v.fz, &v.nodalMass, &v.invMass};
+    for (auto f : nodef) *f += no;
+    double **elemf[19] = {&v.e, &v.p, &v.q, &v.ql, &v.qq, &v.v, &v.volo, &v.vnew, &v.delv,
+                          &v.vdov, &v.arealg, &v.ss, &v.elemMass, &v.delx_xi, &v.delx_eta,
+                          &v.delx_zeta, &v.delv_xi, &v.delv_eta, &v.delv_zeta};
+    for (auto f : elemf) *f += eo;
+    int **conn[7] = {&v.lxim, &v.lxip, &v.letam, &v.letap, &v.lzetam, &v.lzetap, &v.elemBC};
+    for (auto c : conn) *c += eo;
+    v.nodelist += 8 * eo;
+    v.nodelistT += eo;
+    v.nodeElemStart += no;
+    v.nodeElemCornerList += 8 * eo;
+    v.symm += no;
+    v.elemProb += eo;
+    v.nodeProb += no;
+    return v;
+}
+
+// every member's set-up state, built on the device (lg_setup.cu): the
+// topology too when `topology`; then the dt slots and control blocks
+int setup_members(lg_ensemble *en, bool topology)
+{
+    for (int i = 0; i < en->nprob; ++i) {
+        const lg_opts &o = en->opts[i];
+        EN_CUDA(lg::device_setup(member_view(en, i), o.nx, lg::sedov_einit(o.nx, o.einit_factor),
+                                 topology, en->stream, (int)en->eoff[i], (int)en->noff[i], en->E,
+                                 i));
     }
-    std::vector<double> inv;
-    inv.reserve(en->N);
-    for (auto &p : en->prob)
-        for (double m : p.nodalMass) inv.push_back(1.0 / m);
-    if ((st = put(en, en->ds.invMass, inv))) return st;
     const unsigned long long big = [] {
         double v = 1.0e+20;
         unsigned long long b;
@@ -220,6 +240,7 @@ int upload_state(lg_ensemble *en)
         return b;
     }();
     std::vector<unsigned long long> slots(2 * (size_t)en->nprob, big);
+    int st;
     if ((st = put(en, en->ds.dtSlots, slots))) return st;
     EN_CUDA(cudaMemsetAsync(en->ds.gridCounter, 0, sizeof(unsigned), en->stream));
     for (int i = 0; i < en->nprob; ++i) {
@@ -241,43 +262,18 @@ int upload_state(lg_ensemble *en)
     return write_ctl(en);
 }
 
-// concatenated topology with global ids, region order, owners
-int upload_topology(lg_ensemble *en)
+// region order over all members (global element ids, each member's regions
+// in turn) with the EOS repetition counts, and the members' hgcoef
+int upload_regions(lg_ensemble *en)
 {
-    const long long E = en->E, N = en->N;
-    std::vector<int> nl(8 * E), nlT(8 * E), nes(N + 1), ncl(8 * E), conn[6], bc(E), perm(E),
-        rep(E);
-    for (auto &c : conn) c.resize(E);
-    std::vector<uint16_t> eprob(E), nprob(N);
-    std::vector<uint8_t> symm(N, 0);
+    const long long E = en->E;
+    std::vector<int> perm(E), rep(E);
     std::vector<double> hg(en->nprob);
     long long pos = 0;
-    nes[0] = 0;
     for (int pi = 0; pi < en->nprob; ++pi) {
         const lg::Problem &p = en->prob[pi];
-        const long long eo = en->eoff[pi], no = en->noff[pi];
+        const long long eo = en->eoff[pi];
         hg[pi] = p.k.hgcoef;
-        for (int e = 0; e < p.numElem; ++e) {
-            for (int j = 0; j < 8; ++j) {
-                const int g = (int)(p.nodelist[8 * (size_t)e + j] + no);
-                nl[8 * (eo + e) + j] = g;
-                nlT[(size_t)j * E + eo + e] = g;
-            }
-            const std::vector<int> *cs[6] = {&p.lxim, &p.lxip, &p.letam, &p.letap, &p.lzetam,
-                                             &p.lzetap};
-            for (int c = 0; c < 6; ++c) conn[c][eo + e] = (int)((*cs[c])[e] + eo);
-            bc[eo + e] = p.elemBC[e];
-            eprob[eo + e] = (uint16_t)pi;
-        }
-        for (int n = 0; n < p.numNode; ++n) {
-            nes[no + n + 1] = (int)(p.nodeElemStart[n + 1] + 8 * eo);
-            nprob[no + n] = (uint16_t)pi;
-        }
-        for (size_t i = 0; i < p.nodeElemCornerList.size(); ++i)
-            ncl[8 * eo + i] = (int)(p.nodeElemCornerList[i] + 8 * eo);
-        for (int n : p.symmX) symm[no + n] |= 1;
-        for (int n : p.symmY) symm[no + n] |= 2;
-        for (int n : p.symmZ) symm[no + n] |= 4;
         for (int r = 0; r < p.numReg; ++r) {
             const int rr = lg::region_rep(r, p.numReg, p.cost);
             for (int e : p.regElemlist[r]) {
@@ -288,17 +284,9 @@ int upload_topology(lg_ensemble *en)
         }
     }
     if (pos != E) return err(LG_ERR_INVALID, "region sets do not cover all elements");
-    lg::DevState &s = en->ds;
     int st;
-    if ((st = put(en, s.nodelist, nl)) || (st = put(en, s.nodelistT, nlT)) ||
-        (st = put(en, s.nodeElemStart, nes)) || (st = put(en, s.nodeElemCornerList, ncl)) ||
-        (st = put(en, s.lxim, conn[0])) || (st = put(en, s.lxip, conn[1])) ||
-        (st = put(en, s.letam, conn[2])) || (st = put(en, s.letap, conn[3])) ||
-        (st = put(en, s.lzetam, conn[4])) || (st = put(en, s.lzetap, conn[5])) ||
-        (st = put(en, s.elemBC, bc)) || (st = put(en, s.regPerm, perm)) ||
-        (st = put(en, s.regRep, rep)) || (st = put(en, s.symm, symm)) ||
-        (st = put(en, s.elemProb, eprob)) || (st = put(en, s.nodeProb, nprob)) ||
-        (st = put(en, s.hgcoefs, hg)))
+    if ((st = put(en, en->ds.regPerm, perm)) || (st = put(en, en->ds.regRep, rep)) ||
+        (st = put(en, en->ds.hgcoefs, hg)))
         return st;
     return LG_OK;
 }
@@ -387,8 +375,10 @@ int lg_ensemble_create(int nprob, const lg_opts *opts, lg_ensemble **out)
         const lg_opts &o = opts[i];
         if (o.nx < 1 || o.numReg < 1 || o.its < 0 || (long long)o.nx * o.nx * o.nx * 8 > 2147483647LL)
             return fail(err(LG_ERR_INVALID, "problem %d: invalid size", i));
-        en->prob.push_back(
-            lg::build_sedov(o.nx, o.numReg, o.balance, o.cost, o.hgcoef, o.einit_factor));
+        // sizes, constants, time state and regions; the mesh and fields are
+        // built on the device
+        en->prob.push_back(lg::build_sedov_scalars(o.nx, o.numReg, o.balance, o.cost, o.hgcoef,
+                                                   o.einit_factor));
         en->eoff.push_back(en->E);
         en->noff.push_back(en->N);
         en->E += en->prob.back().numElem;
@@ -471,7 +461,7 @@ int lg_ensemble_create(int nprob, const lg_opts *opts, lg_ensemble **out)
     if (cudaMemsetAsync(en->arena, 0, total, en->stream) != cudaSuccess)
         return fail(err(LG_ERR_CUDA, "cudaMemset failed"));
     int st;
-    if ((st = upload_topology(en)) || (st = upload_state(en))) return fail(st);
+    if ((st = upload_regions(en)) || (st = setup_members(en, true))) return fail(st);
     *out = en;
     return LG_OK;
 }
@@ -524,7 +514,7 @@ int lg_ensemble_reset(lg_ensemble *en)
     if (!en) return err(LG_ERR_INVALID, "null handle");
     EN_CUDA(cudaSetDevice(en->device));
     EN_CUDA(cudaStreamSynchronize(en->stream));
-    return upload_state(en);
+    return setup_members(en, false);
 }
 
 int lg_ensemble_info(lg_ensemble *en, long long *total_elems, long long *total_nodes,
@@ -553,15 +543,24 @@ int lg_ensemble_get_field(lg_ensemble *en, int prob, const char *name, void *dst
         EN_CUDA(cudaStreamSynchronize(en->stream));
         return LG_OK;
     }
-    struct { const char *n; std::vector<int> *v; } t[] = {
-        {"nodelist", &p.nodelist}, {"regNumList", &p.regNumList}, {"elemBC", &p.elemBC}};
-    for (auto &f : t)
-        if (!strcmp(f.n, name)) {
-            if (n != f.v->size()) return err(LG_ERR_INVALID, "field '%s' size mismatch", name);
-            memcpy(dst, f.v->data(), n * sizeof(int));
-            return LG_OK;
-        }
-    return err(LG_ERR_INVALID, "unknown field '%s'", name);
+    if (!strcmp(name, "regNumList")) {
+        if (n != p.regNumList.size()) return err(LG_ERR_INVALID, "field '%s' size mismatch", name);
+        memcpy(dst, p.regNumList.data(), n * sizeof(int));
+        return LG_OK;
+    }
+    // topology, member-local ids (the device arrays hold ensemble-wide ids)
+    const bool nl = !strcmp(name, "nodelist");
+    if (!nl && strcmp(name, "elemBC") != 0) return err(LG_ERR_INVALID, "unknown field '%s'", name);
+    const size_t cnt = (nl ? 8 : 1) * (size_t)p.numElem;
+    if (n != cnt) return err(LG_ERR_INVALID, "field '%s' size mismatch", name);
+    const int *src = nl ? en->ds.nodelist + 8 * en->eoff[prob] : en->ds.elemBC + en->eoff[prob];
+    EN_CUDA(cudaMemcpyAsync(dst, src, cnt * sizeof(int), cudaMemcpyDeviceToHost, en->stream));
+    EN_CUDA(cudaStreamSynchronize(en->stream));
+    if (nl) {
+        int *d = static_cast<int *>(dst);
+        for (size_t i = 0; i < cnt; ++i) d[i] -= (int)en->noff[prob];
+    }
+    return LG_OK;
 }
 
 int lg_ensemble_get_scalar(lg_ensemble *en, int prob, const char *name, double *value)

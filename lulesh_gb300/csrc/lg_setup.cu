@@ -18,6 +18,12 @@
 // The region draw stays on the host: it follows the reference's sequential
 // random stream (lulesh-init.cc:401-490) and is uploaded.
 //
+// An ensemble member is set up through a view of the concatenated arrays
+// (every pointer moved to the member's first element or node): the ids it
+// writes are shifted by the member's first element and node, the
+// corner-major nodelist keeps the ensemble's stride, and each element and
+// node records its member.
+//
 // Compiled without FMA contraction: coordinates, volumes and masses must
 // round as the host set-up's do, bit for bit.  The state kernels derive the
 // mesh from the indices, not from the nodelist array, so a reset restores the
@@ -59,7 +65,8 @@ __device__ __forceinline__ long long corners_before(int i)
     return i == 0 ? 0 : 2LL * i - 1;
 }
 
-__global__ void k_setup_topology(DevState s, int nx)
+__global__ void k_setup_topology(DevState s, int nx, int eoff, int noff, long long tstride,
+                                 int pid)
 {
     const int n = nx, en = nx + 1;
     const int E = s.E, N = s.N;
@@ -70,16 +77,17 @@ __global__ void k_setup_topology(DevState s, int nx)
         const int ln[8] = {b, b + 1, b + en + 1, b + en, b + en * en, b + en * en + 1,
                            b + en * en + en + 1, b + en * en + en};
         for (int c = 0; c < 8; ++c) {
-            s.nodelist[8 * (size_t)e + c] = ln[c];
-            s.nodelistT[(size_t)c * E + e] = ln[c];
+            s.nodelist[8 * (size_t)e + c] = ln[c] + noff;
+            s.nodelistT[(size_t)c * tstride + e] = ln[c] + noff;
         }
         // SetupElementConnectivities, lulesh-init.cc:539-565
-        s.lxim[e] = e == 0 ? 0 : e - 1;
-        s.lxip[e] = e == E - 1 ? E - 1 : e + 1;
-        s.letam[e] = e < n ? e : e - n;
-        s.letap[e] = e >= E - n ? e : e + n;
-        s.lzetam[e] = e < nn ? e : e - (int)nn;
-        s.lzetap[e] = e >= E - nn ? e : e + (int)nn;
+        s.lxim[e] = (e == 0 ? 0 : e - 1) + eoff;
+        s.lxip[e] = (e == E - 1 ? E - 1 : e + 1) + eoff;
+        s.letam[e] = (e < n ? e : e - n) + eoff;
+        s.letap[e] = (e >= E - n ? e : e + n) + eoff;
+        s.lzetam[e] = (e < nn ? e : e - (int)nn) + eoff;
+        s.lzetap[e] = (e >= E - nn ? e : e + (int)nn) + eoff;
+        if (s.elemProb) s.elemProb[e] = (uint16_t)pid;
         // SetupBoundaryConditions, lulesh-init.cc:569-673 (one rank: the
         // minimum faces are symmetry planes, the maximum faces free)
         int bc = 0;
@@ -102,15 +110,17 @@ __global__ void k_setup_topology(DevState s, int nx)
         const long long start = corners_before(k) * line * line +
                                 corners_on(k, n) * corners_before(j) * line +
                                 corners_on(k, n) * corners_on(j, n) * corners_before(i);
-        s.nodeElemStart[v] = (int)start;
-        if (v == N - 1) s.nodeElemStart[N] = 8 * E;
+        s.nodeElemStart[v] = (int)(start + 8LL * eoff);
+        if (v == N - 1) s.nodeElemStart[N] = 8 * (E + eoff);
+        if (s.nodeProb) s.nodeProb[v] = (uint16_t)pid;
         int m = 0;
         for (int ek = k - 1; ek <= k; ++ek)
             for (int ej = j - 1; ej <= j; ++ej)
                 for (int ei = i - 1; ei <= i; ++ei) {
                     if (ek < 0 || ek >= n || ej < 0 || ej >= n || ei < 0 || ei >= n) continue;
                     const int el = (ek * n + ej) * n + ei;
-                    s.nodeElemCornerList[start + m++] = 8 * el + corner_of(i - ei, j - ej, k - ek);
+                    s.nodeElemCornerList[start + m++] =
+                        8 * (el + eoff) + corner_of(i - ei, j - ej, k - ek);
                 }
     }
 }
@@ -171,12 +181,16 @@ int blocks_for(long long n)
 
 // Queue the set-up on `stream`: the topology when `topology`, the initial
 // element and node fields always.  s must hold a structured nx^3 mesh's
-// arrays (E = nx^3, N = (nx+1)^3).
+// arrays (E = nx^3, N = (nx+1)^3), or be an ensemble member's view of them:
+// eoff / noff its first element / node, tstride the ensemble's element count
+// (0: s.E), pid its member number.
 cudaError_t device_setup(const DevState &s, int nx, double einit, bool topology,
-                         cudaStream_t stream)
+                         cudaStream_t stream, int eoff, int noff, long long tstride, int pid)
 {
     const long long items = s.E > s.N ? s.E : s.N;
-    if (topology) k_setup_topology<<<blocks_for(items), kSetupBlock, 0, stream>>>(s, nx);
+    if (topology)
+        k_setup_topology<<<blocks_for(items), kSetupBlock, 0, stream>>>(
+            s, nx, eoff, noff, tstride > 0 ? tstride : s.E, pid);
     k_setup_elems<<<blocks_for(s.E), kSetupBlock, 0, stream>>>(s, nx, einit);
     k_setup_nodes<<<blocks_for(s.N), kSetupBlock, 0, stream>>>(s, nx);
     return cudaGetLastError();

@@ -61,3 +61,18 @@ def test_sampled_ensemble_runs(native_lib):
     en = lg.Ensemble(members)
     assert en.step(10) == 0
     assert all(en.scalar(i, "cycle") == 10 for i in range(8))
+
+
+def test_members_set_up_like_single_problems(native_lib):
+    """The device-built ensemble set-up: every member's fields and topology
+    equal the host set-up of the same problem alone, bit for bit."""
+    import lulesh_gb300 as lg
+    en = lg.Ensemble(MEMBERS)
+    for i, m in enumerate(MEMBERS):
+        host = lg.Domain(m["nx"], m["numReg"], m["balance"], m["cost"], hgcoef=m["hgcoef"],
+                         einit_factor=m["einit_factor"], device=-1)
+        for f in lg.NODE_FIELDS + lg.ELEM_FIELDS:
+            assert np.array_equal(_bits(en.field(i, f)), _bits(host.field(f))), (i, f)
+        for f in ("nodelist", "elemBC", "regNumList"):
+            assert np.array_equal(en.field(i, f), host.field(f)), (i, f)
+        assert en.scalar(i, "deltatime") == host.scalar("deltatime")
