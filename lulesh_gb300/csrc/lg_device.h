@@ -50,6 +50,8 @@ struct Ctl {
     double *dt_record;
     int dt_frozen_len;
     int dt_record_len;
+    // the self-check's origin energy, MaxAbsDiff, TotalAbsDiff, MaxRelDiff
+    double verify[4];
 };
 
 struct Params {

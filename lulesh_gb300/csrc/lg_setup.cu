@@ -171,6 +171,59 @@ __global__ void k_setup_nodes(DevState s, int nx)
     }
 }
 
+// The end-of-run self-check of lulesh-util.cc:189-218 on the device: the
+// symmetry of e across the x = y diagonal of plane 0.  k_verify_pairs writes
+// each pair (j, k > j)'s |e(j,k) - e(k,j)| and that over e(k,j) in the
+// reference's loop order; k_verify_reduce takes the maxima (kept only when
+// strictly greater, as the reference keeps them, so 0/0 pairs drop out) and
+// sums the differences serially in that order, so the report's values are
+// the reference's to the bit.
+__device__ __forceinline__ long long pair_pos(int j, int k, int nx)
+{
+    return (long long)j * nx - (long long)j * (j + 1) / 2 + (k - j - 1);
+}
+
+__global__ void k_verify_pairs(const double *e, int nx, double *absd, double *reld)
+{
+    const long long total = (long long)nx * nx;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / nx), k = (int)(idx % nx);
+        if (k <= j) continue;
+        const double a = fabs(e[(size_t)j * nx + k] - e[(size_t)k * nx + j]);
+        const long long p = pair_pos(j, k, nx);
+        absd[p] = a;
+        reld[p] = a / e[(size_t)k * nx + j];
+    }
+}
+
+__global__ void k_verify_reduce(const double *e, int nx, const double *absd, const double *reld,
+                                double *out)
+{
+    __shared__ double sa[kSetupBlock], sr[kSetupBlock];
+    const long long pairs = (long long)nx * (nx - 1) / 2;
+    double ma = 0.0, mr = 0.0;
+    for (long long p = threadIdx.x; p < pairs; p += blockDim.x) {
+        if (ma < absd[p]) ma = absd[p];
+        if (mr < reld[p]) mr = reld[p];
+    }
+    sa[threadIdx.x] = ma;
+    sr[threadIdx.x] = mr;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int t = 1; t < blockDim.x; ++t) {
+            if (ma < sa[t]) ma = sa[t];
+            if (mr < sr[t]) mr = sr[t];
+        }
+        double total = 0.0;
+        for (long long p = 0; p < pairs; ++p) total += absd[p];
+        out[0] = e[0];
+        out[1] = ma;
+        out[2] = total;
+        out[3] = mr;
+    }
+}
+
 int blocks_for(long long n)
 {
     const long long b = (n + kSetupBlock - 1) / kSetupBlock;
@@ -178,6 +231,19 @@ int blocks_for(long long n)
 }
 
 }  // namespace
+
+// Queue the self-check of the energy field e of an nx^3 mesh: out[0..3] =
+// origin energy, MaxAbsDiff, TotalAbsDiff, MaxRelDiff.  scratch holds at
+// least nx * nx doubles.
+cudaError_t device_verify(const double *e, int nx, double *scratch, double *out,
+                          cudaStream_t stream)
+{
+    const long long pairs = (long long)nx * (nx - 1) / 2;
+    double *absd = scratch, *reld = scratch + (pairs > 0 ? pairs : 1);
+    k_verify_pairs<<<blocks_for((long long)nx * nx), kSetupBlock, 0, stream>>>(e, nx, absd, reld);
+    k_verify_reduce<<<1, kSetupBlock, 0, stream>>>(e, nx, absd, reld, out);
+    return cudaGetLastError();
+}
 
 // Queue the set-up on `stream`: the topology when `topology`, the initial
 // element and node fields always.  s must hold a structured nx^3 mesh's

@@ -6,6 +6,8 @@ Domain::Domain by the oracle's golden set-up digests; a host-only handle
 corner lists with kernels; every double field, integer array and time-step
 scalar must equal the host set-up's bit for bit.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -74,3 +76,34 @@ def test_reset_restores_the_setup_state(native_lib):
     assert np.array_equal(d.field("regNumList"), reg2)
     for f, v in init.items():
         assert _same_bits(v, d.field(f)), f
+
+
+def _selfcheck(e, nx):
+    """lulesh-util.cc:189-218, serially, in the reference's loop order"""
+    e = [float(x) for x in e[: nx * nx]]
+    max_abs = total = max_rel = 0.0
+    for j in range(nx):
+        for k in range(j + 1, nx):
+            a = abs(e[j * nx + k] - e[k * nx + j])
+            total += a
+            if max_abs < a:
+                max_abs = a
+            den = e[k * nx + j]
+            if den != 0.0:
+                r = a / den
+            else:  # IEEE: 0/0 is NaN, a/(+-0) is +-inf
+                r = float("nan") if a == 0.0 else math.copysign(float("inf"), den)
+            if max_rel < r:
+                max_rel = r
+    return e[0], max_abs, total, max_rel
+
+
+@pytest.mark.parametrize("nx,cycles", [(1, 3), (30, 100), (150, 40)])
+def test_device_selfcheck_equals_serial_loop(native_lib, nx, cycles):
+    import lulesh_gb300 as lg
+    d = lg.Domain(nx, 11, its=cycles)
+    assert d.run() == 0
+    v = d.verify()
+    ref = _selfcheck(d.field("e"), nx)
+    got = (v["origin_energy"], v["MaxAbsDiff"], v["TotalAbsDiff"], v["MaxRelDiff"])
+    assert got == ref, (got, ref)
