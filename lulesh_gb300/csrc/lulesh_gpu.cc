@@ -8,11 +8,19 @@
 // Additional long options choose the device path:
 //   --precision fp64|fp64-fma|mixed   (default fp64)
 //   --device N
+// and write the final state for visualisation without Silo (which -v needs,
+// as in the reference):
+//   --viz-vtk FILE   the fields of the reference's viz dump (lulesh-viz.cc:
+//                    mesh, regions, e, p, v, q, speed, xd, yd, zd) as a binary
+//                    legacy VTK unstructured grid
 #include <chrono>
+#include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <string>
 #include <vector>
 
 #include "lulesh_gb300.h"
@@ -46,6 +54,7 @@ void usage(const char *exe)
     printf(" -h              : This message\n");
     printf(" --precision <fp64|fp64-fma|mixed> : device arithmetic (def: fp64)\n");
     printf(" --device <n>    : CUDA device ordinal (def: 0)\n");
+    printf(" --viz-vtk <file>: write the final mesh and fields as legacy VTK\n");
     printf("\n\n");
 }
 
@@ -55,6 +64,91 @@ void usage(const char *exe)
     exit(-1);
 }
 
+// legacy VTK binary data is big-endian
+template <typename T>
+void put_be(FILE *f, const std::vector<T> &v)
+{
+    std::vector<unsigned char> b(v.size() * sizeof(T));
+    for (size_t i = 0; i < v.size(); ++i) {
+        unsigned char w[sizeof(T)];
+        memcpy(w, &v[i], sizeof(T));
+        for (size_t k = 0; k < sizeof(T); ++k) b[i * sizeof(T) + k] = w[sizeof(T) - 1 - k];
+    }
+    fwrite(b.data(), 1, b.size(), f);
+}
+
+std::vector<double> get_f64(lg_domain *d, const char *name, size_t n)
+{
+    std::vector<double> v(n);
+    lg_get_field(d, name, v.data(), n);
+    return v;
+}
+
+// The fields of DumpDomainToVisit (lulesh-viz.cc:120-259) -- node
+// coordinates, the hexahedra, the region of each element, e, p, v, q per
+// element and xd, yd, zd and speed per node, the last ones in single
+// precision as the reference writes them -- in a binary legacy VTK file.
+// LULESH's corner order is VTK's hexahedron order.
+int write_vtk(lg_domain *d, const char *path)
+{
+    double ne, nn, cyc, time;
+    lg_get_scalar(d, "numElem", &ne);
+    lg_get_scalar(d, "numNode", &nn);
+    lg_get_scalar(d, "cycle", &cyc);
+    lg_get_scalar(d, "time", &time);
+    const size_t E = (size_t)ne, N = (size_t)nn;
+    FILE *f = fopen(path, "wb");
+    if (!f) return -1;
+    fprintf(f, "# vtk DataFile Version 3.0\nLULESH cycle %d time %.9e\nBINARY\n"
+               "DATASET UNSTRUCTURED_GRID\nPOINTS %zu double\n", (int)cyc, time, N);
+    const std::vector<double> x = get_f64(d, "x", N), y = get_f64(d, "y", N),
+                              z = get_f64(d, "z", N);
+    std::vector<double> xyz(3 * N);
+    for (size_t i = 0; i < N; ++i) {
+        xyz[3 * i] = x[i];
+        xyz[3 * i + 1] = y[i];
+        xyz[3 * i + 2] = z[i];
+    }
+    put_be(f, xyz);
+    std::vector<int32_t> nl(8 * E);
+    lg_get_field(d, "nodelist", nl.data(), nl.size());
+    std::vector<int32_t> cells(9 * E);
+    for (size_t e = 0; e < E; ++e) {
+        cells[9 * e] = 8;
+        for (int j = 0; j < 8; ++j) cells[9 * e + 1 + j] = nl[8 * e + j];
+    }
+    fprintf(f, "\nCELLS %zu %zu\n", E, 9 * E);
+    put_be(f, cells);
+    fprintf(f, "\nCELL_TYPES %zu\n", E);
+    put_be(f, std::vector<int32_t>(E, 12));  // VTK_HEXAHEDRON
+    fprintf(f, "\nCELL_DATA %zu\nSCALARS regions int 1\nLOOKUP_TABLE default\n", E);
+    std::vector<int32_t> reg(E);
+    lg_get_field(d, "regNumList", reg.data(), E);
+    put_be(f, reg);
+    for (const char *name : {"e", "p", "v", "q"}) {
+        fprintf(f, "\nSCALARS %s double 1\nLOOKUP_TABLE default\n", name);
+        put_be(f, get_f64(d, name, E));
+    }
+    const std::vector<double> xd = get_f64(d, "xd", N), yd = get_f64(d, "yd", N),
+                              zd = get_f64(d, "zd", N);
+    std::vector<float> fx(N), fy(N), fz(N), speed(N);
+    for (size_t i = 0; i < N; ++i) {
+        fx[i] = float(xd[i]);
+        fy[i] = float(yd[i]);
+        fz[i] = float(zd[i]);
+        speed[i] = float(std::sqrt((fx[i] * fx[i]) + (fy[i] * fy[i]) + (fz[i] * fz[i])));
+    }
+    fprintf(f, "\nPOINT_DATA %zu\n", N);
+    const std::pair<const char *, const std::vector<float> *> nodal[4] = {
+        {"speed", &speed}, {"xd", &fx}, {"yd", &fy}, {"zd", &fz}};
+    for (auto &v : nodal) {
+        fprintf(f, "SCALARS %s float 1\nLOOKUP_TABLE default\n", v.first);
+        put_be(f, *v.second);
+        fprintf(f, "\n");
+    }
+    return fclose(f) == 0 ? 0 : -1;
+}
+
 }  // namespace
 
 int main(int argc, char *argv[])
@@ -62,6 +156,7 @@ int main(int argc, char *argv[])
     lg_opts o;
     lg_default_opts(&o);
     int showProg = 0, quiet = 0, numFiles = (1 + 10) / 9;
+    const char *vtkPath = nullptr;
     (void)numFiles;
     for (int i = 1; i < argc;) {
         const char *a = argv[i];
@@ -102,6 +197,10 @@ int main(int argc, char *argv[])
         } else if (!strcmp(a, "--device")) {
             int_arg(&o.device, "Missing integer argument to --device",
                     "Parse Error on option --device integer value required after argument\n");
+        } else if (!strcmp(a, "--viz-vtk")) {
+            if (i + 1 >= argc) parse_error("Missing argument to --viz-vtk");
+            vtkPath = argv[i + 1];
+            i += 2;
         } else if (!strcmp(a, "--precision")) {
             if (i + 1 >= argc) parse_error("Missing argument to --precision");
             const char *p = argv[i + 1];
@@ -177,6 +276,11 @@ int main(int argc, char *argv[])
         std::vector<char> buf(4096);
         lg_report(d, elapsed, buf.data(), buf.size());
         std::cout << buf.data();
+    }
+    if (vtkPath && write_vtk(d, vtkPath) != 0) {
+        printf("Error writing out viz file %s\n", vtkPath);
+        lg_destroy(d);
+        return 1;
     }
     lg_destroy(d);
     return 0;
