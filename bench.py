@@ -277,11 +277,32 @@ def run_ensemble(a):
     ms_max = _max_over_ranks(dist, ms)
     value = ws * E * a.steps / (ms_max * 1e3)
 
-    # end to end through the C ABI: upload every member from host memory,
-    # the K cycles, download every member's fields
+    # end to end through the C ABI: upload every member's set-up state from
+    # pinned host memory, the K cycles, download every member's fields
     fields = lg.NODE_FIELDS + lg.ELEM_FIELDS
-    t0 = time.perf_counter()
+    try:
+        import torch
+        pinned = torch.cuda.is_available()
+    except ImportError:
+        torch, pinned = None, False
     en.reset()
+    host = []
+    for i in range(len(members)):
+        row = {}
+        for f in fields:
+            v = en.field(i, f)
+            if pinned:
+                buf = torch.empty(v.size, dtype=torch.float64, pin_memory=True).numpy()
+                buf[:] = v
+                v = buf
+            row[f] = v
+        host.append(row)
+    h2d = sum(v.nbytes for row in host for v in row.values())
+    _barrier(dist)
+    t0 = time.perf_counter()
+    for i, row in enumerate(host):
+        for f, v in row.items():
+            en.set_field(i, f, v)
     en.step(a.steps)
     d2h = 0
     for i in range(len(members)):
@@ -289,7 +310,7 @@ def run_ensemble(a):
             d2h += en.field(i, f).nbytes
     t_e2e = _max_over_ranks(dist, time.perf_counter() - t0)
     e2e = {"value": ws * E * a.steps / (t_e2e * 1e6), "unit": UNIT,
-           "h2d_bytes_per_step": d2h / a.steps, "d2h_bytes_per_step": d2h / a.steps}
+           "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps}
 
     # the plain path, member by member (device time of each member's cycles)
     seq_ms = 0.0
@@ -454,12 +475,31 @@ def run_gpu(a):
            "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": h2d / a.steps,
            "status": st2}
 
+    # the same when the caller keeps the reference's Domain on the host and
+    # syncs it around every cycle (the second binding of the integration
+    # guide): every field up, one cycle, every field down, a few cycles
+    nsync = min(a.steps, 10)
+    d.reset()
+    _barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(nsync):
+        for f in fields:
+            d.set_field(f, host[f])
+        d.step(1)
+        for f in fields:
+            d.field(f, out=host[f])
+    t_sync = _max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_host = {"value": ws * E * nsync / (t_sync * 1e6), "unit": UNIT, "cycles": nsync,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                "how": "every Domain field from pinned host memory, lg_step(1), every field "
+                       "back, per cycle"}
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if a.precision != "mixed" else "f64+f32",
             "data": "synthetic: the reference's built-in Sedov problem set-up",
-            "config": _workload(a), "e2e": e2e, "gpu_launches": launches,
-            "roofline": roofline, "roofline_fp64": roof64, "clocks": clk.summary(),
+            "config": _workload(a), "e2e": e2e, "e2e_host_domain": e2e_host,
+            "gpu_launches": launches, "roofline": roofline, "roofline_fp64": roof64, "clocks": clk.summary(),
             "origin_energy": verify["origin_energy"]}
     if a.err_vs_fp64 and a.precision != "fp64":
         line["err_vs_fp64"] = error_vs_fp64(a, d)

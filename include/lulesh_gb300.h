@@ -207,6 +207,10 @@ int lg_ensemble_info(lg_ensemble *en, long long *total_elems, long long *total_n
  * and scalars (time deltatime dtcourant dthydro cycle status numElem numNode
  * nx numReg hgcoef einit_factor its). */
 int lg_ensemble_get_field(lg_ensemble *en, int prob, const char *name, void *dst, size_t n);
+/* Replace member prob's double accessor field `name` (n values from host
+ * memory), e.g. the initial energies of a study; nodalMass also updates the
+ * mixed path's reciprocal.  Integer topology is fixed at creation. */
+int lg_ensemble_set_field(lg_ensemble *en, int prob, const char *name, const void *src, size_t n);
 int lg_ensemble_get_scalar(lg_ensemble *en, int prob, const char *name, double *value);
 
 /* Times every block size (64, 128, 256) and grid shape (one pass over the

@@ -110,6 +110,8 @@ def load() -> ctypes.CDLL:
     lib.lg_ensemble_info.argtypes = [H] + [ctypes.POINTER(ctypes.c_longlong)] * 3
     lib.lg_ensemble_get_field.argtypes = [H, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p,
                                           ctypes.c_size_t]
+    lib.lg_ensemble_set_field.argtypes = [H, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p,
+                                          ctypes.c_size_t]
     lib.lg_ensemble_get_scalar.argtypes = [H, ctypes.c_int, ctypes.c_char_p,
                                            ctypes.POINTER(ctypes.c_double)]
     lib.lg_ensemble_autotune.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
@@ -445,3 +447,10 @@ class Ensemble:
         if st:
             _raise(st, self._lib)
         return out
+
+    def set_field(self, member: int, name: str, values) -> None:
+        """Replace a member's double field (lg_ensemble_set_field)."""
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        st = self._lib.lg_ensemble_set_field(self._h, member, name.encode(), a.ctypes.data, a.size)
+        if st:
+            _raise(st, self._lib)

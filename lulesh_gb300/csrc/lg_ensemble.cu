@@ -563,6 +563,30 @@ int lg_ensemble_get_field(lg_ensemble *en, int prob, const char *name, void *dst
     return LG_OK;
 }
 
+int lg_ensemble_set_field(lg_ensemble *en, int prob, const char *name, const void *src, size_t n)
+{
+    if (!en || !name || prob < 0 || prob >= en->nprob || (!src && n))
+        return err(LG_ERR_INVALID, "invalid argument");
+    EN_CUDA(cudaSetDevice(en->device));
+    lg::Problem &p = en->prob[prob];
+    bool node = false;
+    if (!host_f64(p, name, &node))
+        return err(LG_ERR_INVALID, "'%s' is not a double field of a member", name);
+    const size_t cnt = node ? p.numNode : p.numElem;
+    if (n != cnt) return err(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, cnt, n);
+    double *dst = dev_f64(en->ds, name) + (node ? en->noff[prob] : en->eoff[prob]);
+    EN_CUDA(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, en->stream));
+    if (!strcmp(name, "nodalMass")) {
+        const double *m = static_cast<const double *>(src);
+        std::vector<double> inv(cnt);
+        for (size_t i = 0; i < cnt; ++i) inv[i] = 1.0 / m[i];
+        EN_CUDA(cudaMemcpyAsync(en->ds.invMass + en->noff[prob], inv.data(), cnt * sizeof(double),
+                                cudaMemcpyHostToDevice, en->stream));
+    }
+    EN_CUDA(cudaStreamSynchronize(en->stream));
+    return LG_OK;
+}
+
 int lg_ensemble_get_scalar(lg_ensemble *en, int prob, const char *name, double *value)
 {
     if (!en || !name || !value || prob < 0 || prob >= en->nprob)

@@ -76,3 +76,26 @@ def test_members_set_up_like_single_problems(native_lib):
         for f in ("nodelist", "elemBC", "regNumList"):
             assert np.array_equal(en.field(i, f), host.field(f)), (i, f)
         assert en.scalar(i, "deltatime") == host.scalar("deltatime")
+
+
+def test_set_field_of_a_member(native_lib):
+    """A member whose energy field is replaced evolves as the single problem
+    given the same field; the other members are untouched."""
+    import lulesh_gb300 as lg
+    en = lg.Ensemble(MEMBERS)
+    m = MEMBERS[1]
+    e = en.field(1, "e")
+    e[: 50] += 0.25 * e[0]
+    en.set_field(1, "e", e)
+    assert en.step(20) == 0
+    d = lg.Domain(m["nx"], m["numReg"], m["balance"], m["cost"], its=m["its"],
+                  hgcoef=m["hgcoef"], einit_factor=m["einit_factor"])
+    d.set_field("e", e)
+    assert d.step(20) == 0
+    for f in ("e", "p", "x", "xd"):
+        assert np.array_equal(_bits(en.field(1, f)), _bits(d.field(f))), f
+    ref = lg.Ensemble(MEMBERS)
+    assert ref.step(20) == 0
+    assert np.array_equal(_bits(en.field(0, "e")), _bits(ref.field(0, "e")))
+    with pytest.raises(Exception):
+        en.set_field(1, "nodelist", np.zeros(8 * m["nx"] ** 3))
