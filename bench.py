@@ -64,9 +64,8 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 
 # FP64 thread-instructions (DADD + DMUL + DFMA) per element per launch,
 # from an ncu capture of each kernel of the strict and the FMA build at
-# s=100 (profiles/leapfrog_fp64_s100_ncu.md; k_nodes: per node, stored per
-# element at s=100's N/E; k_material: the s=100 region mix); absent where
-# not measured.
+# s=100, 11 regions (k_nodes: counted per node, stored per element at
+# s=100's N/E; k_material: the s=100 region mix); absent where not measured.
 FP64_INST_PER_ELEM = {
     "fp64": {"k_forces": 1363, "k_kinematics": 728, "k_material": 770,
              "k_nodes": 113 * 1030301 / 1000000},
@@ -78,8 +77,8 @@ FP64_INST_PER_ELEM = {
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element per
 # launch (k_nodes: per node), from one ncu capture of each kernel on a smaller
 # mesh of the same problem, scaled to the benchmarked mesh by the units it
-# processes: s=100 for the FP64 builds, s=96 r16 b2 c4 for the mixed one
-# (profiles/).  Well above the algorithmic bytes: the per-corner force
+# processes: s=100 for the FP64 builds, s=96 r16 b2 c4 for the mixed one.
+# Well above the algorithmic bytes: the per-corner force
 # scratch (k_forces writes, k_nodes reads) and the region-order gathers of
 # k_material.
 TRAFFIC_PER_UNIT = {
