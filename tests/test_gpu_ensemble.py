@@ -99,3 +99,29 @@ def test_set_field_of_a_member(native_lib):
     assert np.array_equal(_bits(en.field(0, "e")), _bits(ref.field(0, "e")))
     with pytest.raises(Exception):
         en.set_field(1, "nodelist", np.zeros(8 * m["nx"] ** 3))
+
+
+def test_one_member_fails_alone(native_lib):
+    """Failure detection without a GPU fault: one member's first element is
+    inverted on the host (a node's x moved past its neighbour), so that
+    member stops with VolumeError (-1) on its first cycle; the others run on
+    exactly as in an ensemble without the planted error."""
+    import lulesh_gb300 as lg
+    bad = 2
+    en = lg.Ensemble(MEMBERS)
+    x = en.field(bad, "x")
+    h = x[1] - x[0]
+    x[1] = x[0] - 5.0 * h          # node 1 of element 0 now left of node 0
+    en.set_field(bad, "x", x)
+    assert en.step(20) == -1       # the first member in error
+    assert en.scalar(bad, "status") == -1
+    assert en.scalar(bad, "cycle") <= 1
+    clean = lg.Ensemble(MEMBERS)
+    assert clean.step(20) == 0
+    for i in range(len(MEMBERS)):
+        if i == bad:
+            continue
+        assert en.scalar(i, "status") == 0
+        assert en.scalar(i, "cycle") == clean.scalar(i, "cycle")
+        for f in ("e", "x", "xd"):
+            assert np.array_equal(_bits(en.field(i, f)), _bits(clean.field(i, f))), (i, f)
