@@ -87,7 +87,7 @@ LG_HD void volu_der_vjp(const double *x, const double *y, const double *z, const
     for (int i = 0; i < 6; ++i) {
         const int p0 = m[P[i][0]], p1 = m[P[i][1]], q0 = m[Q[i][0]], q1 = m[Q[i][1]];
         const double Xp = x[p0] + x[p1], Yp = y[p0] + y[p1];
-        const double Xq = x[q0] + x[q1], Yq = y[q0] + y[q1], Zq = z[q0] + z[q1];
+        const double Xq = x[q0] + x[q1], Zq = z[q0] + z[q1];
         const double ts = t * S[i];
         const double gYp = ts * (a * Zq - c * Xq);
         const double gZq = ts * (a * Yp - b * Xp);

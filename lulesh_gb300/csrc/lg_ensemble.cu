@@ -192,10 +192,6 @@ double *dev_f64(lg::DevState &s, const char *name)
     return nullptr;
 }
 
-const char *kFields[26] = {"x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx",
-                           "fy", "fz", "nodalMass", "e", "p", "q", "ql", "qq", "v", "volo",
-                           "vnew", "delv", "vdov", "arealg", "ss", "elemMass"};
-
 // member i's view of the concatenated arrays: every pointer moved to its
 // first element or node, its own sizes
 lg::DevState member_view(const lg_ensemble *en, int i)
