@@ -171,6 +171,17 @@ int lg_dt_freeze(lg_domain *d, const double *dts, int n);
 int lg_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask, double *J,
                double *dJ_de0, double *dJ_dhgcoef);
 
+/* The general reverse-mode product of the same cycles: given the adjoint of
+ * the final state, field by field -- seed[f] for f in x y z xd yd zd
+ * (numNode values each) then e p q v ss (numElem each), NULL for a zero
+ * seed -- returns the adjoint of the current (initial) state in grad[f]
+ * (NULL: not wanted) and dJ/dhgcoef.  For an objective J(final state), seed
+ * with dJ/d(final fields).  lg_adjoint is the seed e = mask * volo.  Same
+ * frozen-step and precision conditions; leaves the handle in the final
+ * state. */
+int lg_adjoint_vjp(lg_domain *d, int ncycles, int ckpt_k, const double *const seed[11],
+                   double *const grad[11], double *dJ_dhgcoef);
+
 /* ---------------------------------------------------------------------------
  * Ensembles: many independent problems advanced together.  No counterpart in
  * the reference, which runs one problem per process; each member behaves as

@@ -35,6 +35,8 @@ NODE_FIELDS = ["x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy",
                "nodalMass"]
 ELEM_FIELDS = ["e", "p", "q", "ql", "qq", "v", "volo", "vnew", "delv", "vdov", "arealg",
                "ss", "elemMass"]
+# the state the adjoint carries, in lg_adjoint_vjp's seed / gradient order
+ADJOINT_FIELDS = ["x", "y", "z", "xd", "yd", "zd", "e", "p", "q", "v", "ss"]
 
 
 class LuleshError(RuntimeError):
@@ -101,6 +103,9 @@ def load() -> ctypes.CDLL:
     lib.lg_adjoint.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_ubyte),
                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double)]
+    P11 = ctypes.c_void_p * 11
+    lib.lg_adjoint_vjp.argtypes = [H, ctypes.c_int, ctypes.c_int, P11, P11,
+                                   ctypes.POINTER(ctypes.c_double)]
     lib.lg_ensemble_sample.argtypes = [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(_Opts)]
     lib.lg_ensemble_create.argtypes = [ctypes.c_int, ctypes.POINTER(_Opts), ctypes.POINTER(H)]
     lib.lg_ensemble_destroy.argtypes = [H]
@@ -251,6 +256,36 @@ class Domain:
         if st:
             _raise(st, self._lib)
         return J.value, ge, gh.value
+
+    def adjoint_vjp(self, ncycles: int, seeds: dict, want=ADJOINT_FIELDS,
+                    ckpt: int = 20) -> tuple[dict, float]:
+        """Reverse-mode product of ncycles frozen-dt cycles from the current
+        state (lg_adjoint_vjp): seeds maps final-state field names (of
+        ADJOINT_FIELDS) to dJ/d(final field); returns {name: dJ/d(initial
+        field)} for the names in `want`, and dJ/dhgcoef."""
+        seed_arr = (ctypes.c_void_p * 11)()
+        keep = []
+        for name, v in seeds.items():
+            if name not in ADJOINT_FIELDS:
+                raise KeyError(f"{name} is not one of {ADJOINT_FIELDS}")
+            n = self.numNode if name in NODE_FIELDS else self.numElem
+            a = np.ascontiguousarray(v, dtype=np.float64)
+            if a.size != n:
+                raise ValueError(f"seed {name}: expected {n} values, got {a.size}")
+            keep.append(a)
+            seed_arr[ADJOINT_FIELDS.index(name)] = a.ctypes.data
+        grad_arr = (ctypes.c_void_p * 11)()
+        grads = {}
+        for name in want:
+            n = self.numNode if name in NODE_FIELDS else self.numElem
+            grads[name] = np.empty(n, dtype=np.float64)
+            grad_arr[ADJOINT_FIELDS.index(name)] = grads[name].ctypes.data
+        gh = ctypes.c_double()
+        st = self._lib.lg_adjoint_vjp(self._h, int(ncycles), int(ckpt), seed_arr, grad_arr,
+                                      ctypes.byref(gh))
+        if st:
+            _raise(st, self._lib)
+        return grads, gh.value
 
     def phase(self, which: int) -> int:
         return self._status(self._lib.lg_phase(self._h, int(which)), False)

@@ -1,11 +1,13 @@
-"""Terminal-energy objective of the leap-frog path as a torch.autograd.Function.
+"""The leap-frog path as torch.autograd.Functions.
 
-A thin binding over the C ABI's lg_adjoint: the forward evaluates
-J(e0, hgcoef) -- the total internal energy sum(e * volo) of a fixed set of
-elements after a fixed number of cycles with a frozen time-step sequence,
-starting from the initial energy field e0 -- and the backward returns the
-gradients the hand-written adjoint computed in the same call.  Tensors live
-on the host; the GPU work happens inside the library.
+Thin bindings over the C ABI's adjoint:
+  TerminalEnergy    J(e0, hgcoef), the total internal energy sum(e * volo) of a
+                    fixed set of elements after a fixed number of cycles with a
+                    frozen time-step sequence, from the initial energy field
+                    e0; the forward also computes the gradients (lg_adjoint);
+  FinalEnergyField  the final energy field e(e0, hgcoef) itself, so that any
+                    torch loss of it backpropagates (lg_adjoint_vjp).
+Tensors live on the host; the GPU work happens inside the library.
 """
 from __future__ import annotations
 
@@ -62,6 +64,25 @@ class TerminalEnergyProblem:
         d.set_scalar("hgcoef", hgcoef)
         return d.adjoint(self.ncycles, self.mask, self.ckpt)
 
+    def final_field(self, e0: np.ndarray, hgcoef: float, name: str = "e") -> np.ndarray:
+        """A field of the final state after the frozen-step cycles from e0."""
+        d = self.dom
+        d.reset()
+        d.set_field("e", e0)
+        d.set_scalar("hgcoef", hgcoef)
+        if d.step(self.ncycles) != 0:
+            raise RuntimeError("forward run failed")
+        return d.field(name)
+
+    def vjp(self, e0: np.ndarray, hgcoef: float, seeds: dict, want=("e",)):
+        """dJ/d(initial fields in `want`) and dJ/dhgcoef for an objective J of
+        the final state whose gradient is `seeds` (lg_adjoint_vjp)."""
+        d = self.dom
+        d.reset()
+        d.set_field("e", e0)
+        d.set_scalar("hgcoef", hgcoef)
+        return d.adjoint_vjp(self.ncycles, seeds, want, self.ckpt)
+
 
 def centroid_mask(dom: Domain, radius: float) -> np.ndarray:
     nl = dom.field("nodelist").reshape(-1, 8)
@@ -82,3 +103,21 @@ class TerminalEnergy(torch.autograd.Function):
     def backward(ctx, gJ):
         ge, gh = ctx.saved_tensors
         return gJ * ge, gJ * gh, None
+
+
+class FinalEnergyField(torch.autograd.Function):
+    """The final energy field e(e0, hgcoef) of a TerminalEnergyProblem's
+    cycles, differentiable in both: any torch loss of the final field
+    backpropagates through lg_adjoint_vjp."""
+
+    @staticmethod
+    def forward(ctx, e0: torch.Tensor, hgcoef: torch.Tensor, problem: TerminalEnergyProblem):
+        e0n = e0.detach().cpu().double().numpy().copy()
+        ctx.problem, ctx.e0, ctx.hg = problem, e0n, float(hgcoef)
+        return torch.from_numpy(problem.final_field(e0n, float(hgcoef)).copy())
+
+    @staticmethod
+    def backward(ctx, g):
+        seed = g.detach().cpu().double().numpy()
+        grads, gh = ctx.problem.vjp(ctx.e0, ctx.hg, {"e": seed}, want=("e",))
+        return torch.from_numpy(grads["e"]), torch.tensor(gh, dtype=torch.float64), None

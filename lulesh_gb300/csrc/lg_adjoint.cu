@@ -26,6 +26,7 @@
 #include <cstring>
 #include <vector>
 
+#include "lg_adjoint.h"
 #include "lg_adjoint_cycle.h"
 #include "lg_device.h"
 #include "lg_kernelset.h"
@@ -113,23 +114,9 @@ int err(int code, const char *fmt, ...)
 
 }  // namespace
 
-// Internal entry point used by lg_api.cu's lg_adjoint (which owns the handle).
 namespace lg {
 
-// (must match the declaration in lg_api.cu)
-struct AdjointIO {
-    const DevState *ds;
-    const KernelSet *ks;
-    cudaStream_t stream;
-    Ctl *h_ctl;                 // pinned host copy of the control block
-    const double *dts;          // host: frozen time steps of the cycles run
-    int ncycles, ckpt_k;
-    const unsigned char *mask;  // host, E entries
-    double hgcoef;
-    const std::vector<int> *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *elemBC;
-};
-
-int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg)
+int adjoint_run(const AdjointIO &io, double *J, double *dJdhg)
 {
     const DevState &S = *io.ds;
     const int E = S.E, N = S.N;
@@ -260,23 +247,33 @@ int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg)
     if (cend.status != 0) return cend.status;
     if ((rc = save(ckpt + (size_t)nseg * snapD))) return rc;
 
-    // objective: sum of e * volo over the masked elements of the final state
-    {
+    // the adjoint of the final state: the masked terminal energy sum(e * volo)
+    // seeds e with volo on the masked elements; otherwise the caller's seeds
+    AD_CUDA(cudaMemsetAsync(nbar, 0, 8 * 6 * (size_t)N, st));
+    AD_CUDA(cudaMemsetAsync(ebar, 0, 8 * 5 * (size_t)E, st));
+    AD_CUDA(cudaMemsetAsync(hgAcc, 0, 8, st));
+    if (io.mask) {
         std::vector<double> e(E), volo(E);
         AD_CUDA(cudaMemcpyAsync(e.data(), S.e, 8 * (size_t)E, cudaMemcpyDeviceToHost, st));
         AD_CUDA(cudaMemcpyAsync(volo.data(), S.volo, 8 * (size_t)E, cudaMemcpyDeviceToHost, st));
         AD_CUDA(cudaStreamSynchronize(st));
         double j = 0.;
-        std::vector<double> eb0(5 * (size_t)E, 0.);
+        std::vector<double> eb0(E, 0.);
         for (int i = 0; i < E; ++i)
             if (io.mask[i]) {
                 j += e[i] * volo[i];
                 eb0[i] = volo[i];
             }
-        *J = j;
-        AD_CUDA(cudaMemsetAsync(nbar, 0, 8 * 6 * (size_t)N, st));
-        AD_CUDA(cudaMemcpyAsync(ebar, eb0.data(), 8 * eb0.size(), cudaMemcpyHostToDevice, st));
-        AD_CUDA(cudaMemsetAsync(hgAcc, 0, 8, st));
+        if (J) *J = j;
+        AD_CUDA(cudaMemcpyAsync(ebar, eb0.data(), 8 * (size_t)E, cudaMemcpyHostToDevice, st));
+    } else {
+        for (int f = 0; f < kAdjFields; ++f) {
+            if (!io.seed || !io.seed[f]) continue;
+            double *dst = f < 6 ? nbar + (size_t)f * N : ebar + (size_t)(f - 6) * E;
+            AD_CUDA(cudaMemcpyAsync(dst, io.seed[f], 8 * (size_t)(f < 6 ? N : E),
+                                    cudaMemcpyHostToDevice, st));
+        }
+        AD_CUDA(cudaStreamSynchronize(st));  // the seeds are the caller's memory
     }
 
     AdjArgs A;
@@ -304,7 +301,7 @@ int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg)
         const int cb = sg * K, ce = std::min(cb + K, io.ncycles);
         if ((rc = restore(ckpt + (size_t)sg * snapD))) return rc;
         Ctl cs = ckctl[sg];
-        cs.cycle_limit = ce;
+        cs.cycle_limit = c0.cycle + ce;  // absolute, like the cycle counter
         if ((rc = write_ctl(cs))) return rc;
         for (int c = cb; c < ce; ++c) {
             if ((rc = save(seg + (size_t)(c - cb) * snapD))) return rc;
@@ -314,6 +311,11 @@ int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg)
                                         8 * (size_t)E, cudaMemcpyDeviceToDevice, st));
         }
         if ((rc = save(seg + (size_t)(ce - cb) * snapD))) return rc;
+        Ctl cr;
+        if ((rc = read_ctl(&cr))) return rc;
+        if (cr.status != 0 || cr.cycle != c0.cycle + ce)
+            return err(LG_ERR_STATE, "adjoint: the recomputed segment ended at cycle %d (status %d), "
+                                     "not %d", cr.cycle, cr.status, c0.cycle + ce);
         for (int c = ce - 1; c >= cb; --c) {
             A.s0 = snap_at(seg + (size_t)(c - cb) * snapD);
             A.s1 = snap_at(seg + (size_t)(c - cb + 1) * snapD);
@@ -329,7 +331,12 @@ int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg)
         }
         AD_CUDA(cudaGetLastError());
     }
-    AD_CUDA(cudaMemcpyAsync(dJde, ebar, 8 * (size_t)E, cudaMemcpyDeviceToHost, st));
+    for (int f = 0; f < kAdjFields; ++f) {
+        if (!io.grad || !io.grad[f]) continue;
+        const double *src = f < 6 ? nbar + (size_t)f * N : ebar + (size_t)(f - 6) * E;
+        AD_CUDA(cudaMemcpyAsync(io.grad[f], src, 8 * (size_t)(f < 6 ? N : E),
+                                cudaMemcpyDeviceToHost, st));
+    }
     AD_CUDA(cudaMemcpyAsync(dJdhg, hgAcc, 8, cudaMemcpyDeviceToHost, st));
     // leave the handle in the final forward state
     if ((rc = restore(ckpt + (size_t)nseg * snapD))) return rc;

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "lg_device.h"
+#include "lg_adjoint.h"
 #include "lg_kernelset.h"
 #include "lg_problem.h"
 #include "lulesh_gb300.h"
@@ -85,18 +86,6 @@ struct lg_domain {
 };
 
 namespace lg {
-struct AdjointIO {
-    const DevState *ds;
-    const KernelSet *ks;
-    cudaStream_t stream;
-    Ctl *h_ctl;
-    const double *dts;
-    int ncycles, ckpt_k;
-    const unsigned char *mask;
-    double hgcoef;
-    const std::vector<int> *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *elemBC;
-};
-int adjoint_run(const AdjointIO &io, double *J, double *dJde, double *dJdhg);
 cudaError_t device_setup(const DevState &s, int nx, double einit, bool topology,
                          cudaStream_t stream, int eoff = 0, int noff = 0, long long tstride = 0,
                          int pid = 0);
@@ -935,11 +924,12 @@ int lg_dt_freeze(lg_domain *d, const double *dts, int n)
     return write_ctl(d);
 }
 
-int lg_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask, double *J,
-               double *dJ_de0, double *dJ_dhgcoef)
+namespace {
+
+// lg_adjoint and lg_adjoint_vjp: checks, then the checkpointed sweep
+int run_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask,
+                const double *const *seed, double *const *grad, double *J, double *dJ_dhgcoef)
 {
-    if (!d || ncycles < 1 || ckpt_k < 1 || !mask || !J || !dJ_de0 || !dJ_dhgcoef)
-        return set_error(LG_ERR_INVALID, "invalid argument");
     if (d->opts.precision == LG_MIXED)
         return set_error(LG_ERR_INVALID, "the adjoint differentiates the FP64 paths only");
     int st;
@@ -948,17 +938,37 @@ int lg_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask,
     if (d->h_ctl->status != 0) return d->h_ctl->status;
     const int c0 = d->h_ctl->cycle;
     if (!d->d_dtfrozen || c0 + ncycles > d->dtfrozen_len)
-        return set_error(LG_ERR_STATE, "lg_adjoint needs frozen time steps for cycles %d..%d "
+        return set_error(LG_ERR_STATE, "the adjoint needs frozen time steps for cycles %d..%d "
                                        "(lg_dt_freeze)", c0, c0 + ncycles - 1);
     drop_graphs(d);  // the adjoint launches its own cycles
     if ((st = ensure_topology_mirror(d))) return st;
     const lg::Problem &p = d->prob;
     lg::AdjointIO io{&d->ds, d->ks, d->stream, d->h_ctl, d->h_dtfrozen.data() + c0, ncycles,
-                     ckpt_k, mask, d->ds.prm.hgcoef, &p.lxim, &p.lxip, &p.letam, &p.letap,
-                     &p.lzetam, &p.lzetap, &p.elemBC};
-    st = lg::adjoint_run(io, J, dJ_de0, dJ_dhgcoef);
+                     ckpt_k, mask, seed, grad, d->ds.prm.hgcoef, &p.lxim, &p.lxip, &p.letam,
+                     &p.letap, &p.lzetam, &p.lzetap, &p.elemBC};
+    st = lg::adjoint_run(io, J, dJ_dhgcoef);
     d->launches += 10LL * ncycles;
     return st;
+}
+
+}  // namespace
+
+int lg_adjoint(lg_domain *d, int ncycles, int ckpt_k, const unsigned char *mask, double *J,
+               double *dJ_de0, double *dJ_dhgcoef)
+{
+    if (!d || ncycles < 1 || ckpt_k < 1 || !mask || !J || !dJ_de0 || !dJ_dhgcoef)
+        return set_error(LG_ERR_INVALID, "invalid argument");
+    double *grad[lg::kAdjFields] = {};
+    grad[6] = dJ_de0;
+    return run_adjoint(d, ncycles, ckpt_k, mask, nullptr, grad, J, dJ_dhgcoef);
+}
+
+int lg_adjoint_vjp(lg_domain *d, int ncycles, int ckpt_k, const double *const seed[11],
+                   double *const grad[11], double *dJ_dhgcoef)
+{
+    if (!d || ncycles < 1 || ckpt_k < 1 || !seed || !grad || !dJ_dhgcoef)
+        return set_error(LG_ERR_INVALID, "invalid argument");
+    return run_adjoint(d, ncycles, ckpt_k, nullptr, seed, grad, nullptr, dJ_dhgcoef);
 }
 
 int lg_profile(lg_domain *d, int ncycles, double *ms, const char **names, int *nkernels)

@@ -21,24 +21,11 @@
 #include <random>
 #include <vector>
 
-#include "lg_adjoint_cycle.h"
-#include "lulesh_oracle.h"
+#include "adjoint_host.h"
 
-using namespace lg;
+using hostadj::fld;
+using hostadj::ifld;
 using std::vector;
-
-static vector<double> fld(orc_domain *d, const char *n)
-{
-    size_t c;
-    double *p = orc_field_f64(d, n, &c);
-    return vector<double>(p, p + c);
-}
-static vector<int> ifld(orc_domain *d, const char *n)
-{
-    size_t c;
-    int *p = orc_field_i32(d, n, &c);
-    return vector<int>(p, p + c);
-}
 
 struct Run {
     int nx, nreg, ncyc;
@@ -119,15 +106,9 @@ int main(int argc, char **argv)
         orc_destroy(d);
     }
 
-    // forward with stored states and temporaries
+    // forward with stored states and temporaries, then the reverse sweep
     orc_domain *d = fresh(r, r.e0, r.hg);
-    const int E = r.nx * r.nx * r.nx, N = (r.nx + 1) * (r.nx + 1) * (r.nx + 1);
-    const char *nodeF[6] = {"x", "y", "z", "xd", "yd", "zd"};
-    const char *elemF[5] = {"e", "p", "q", "v", "ss"};
-    const char *tempF[8] = {"vnew", "vdov", "delx_xi", "delx_eta", "delx_zeta",
-                            "delv_xi", "delv_eta", "delv_zeta"};
-    const size_t snapD = 6 * (size_t)N + 5 * (size_t)E;
-    vector<double> snaps((r.ncyc + 1) * snapD), temps(r.ncyc * 8 * (size_t)E);
+    const int E = r.nx * r.nx * r.nx;
     const bool branch = getenv("LG_FD_BRANCH") && atoi(getenv("LG_FD_BRANCH"));
     if (branch) {
         if (orc_tape_record(d, r.ncyc) != 0) {
@@ -136,115 +117,12 @@ int main(int argc, char **argv)
         }
         g_tape = d;
     }
-    auto save = [&](int c) {
-        double *b = &snaps[c * snapD];
-        for (int i = 0; i < 6; ++i) {
-            const vector<double> f = fld(d, nodeF[i]);
-            memcpy(b + (size_t)i * N, f.data(), 8 * (size_t)N);
-        }
-        for (int i = 0; i < 5; ++i) {
-            const vector<double> f = fld(d, elemF[i]);
-            memcpy(b + 6 * (size_t)N + (size_t)i * E, f.data(), 8 * (size_t)E);
-        }
-    };
-    for (int c = 0; c < r.ncyc; ++c) {
-        save(c);
-        orc_step(d, 1);
-        for (int t = 0; t < 8; ++t) {
-            const vector<double> f = fld(d, tempF[t]);
-            memcpy(&temps[(c * 8 + t) * (size_t)E], f.data(), 8 * (size_t)E);
-        }
-    }
-    save(r.ncyc);
-
-    // host DevState for the item functions
-    DevState s{};
-    s.E = E;
-    s.N = N;
-    vector<double> volo = fld(d, "volo"), mass = fld(d, "elemMass"), nmass = fld(d, "nodalMass");
-    vector<int> nl = ifld(d, "nodelist"), nlT(8 * (size_t)E);
-    for (int k = 0; k < E; ++k)
-        for (int j = 0; j < 8; ++j) nlT[(size_t)j * E + k] = nl[8 * k + j];
-    vector<int> nes = ifld(d, "nodeElemStart"), ncl = ifld(d, "nodeElemCornerList");
-    vector<int> lxim = ifld(d, "lxim"), lxip = ifld(d, "lxip"), letam = ifld(d, "letam"),
-                letap = ifld(d, "letap"), lzetam = ifld(d, "lzetam"), lzetap = ifld(d, "lzetap"),
-                bc = ifld(d, "elemBC");
-    vector<uint8_t> symm(N, 0);
-    for (int v : ifld(d, "symmX")) symm[v] |= 1;
-    for (int v : ifld(d, "symmY")) symm[v] |= 2;
-    for (int v : ifld(d, "symmZ")) symm[v] |= 4;
-    s.volo = volo.data();
-    s.elemMass = mass.data();
-    s.nodalMass = nmass.data();
-    s.nodelistT = nlT.data();
-    s.nodeElemStart = nes.data();
-    s.nodeElemCornerList = ncl.data();
-    s.lxim = lxim.data(); s.lxip = lxip.data(); s.letam = letam.data(); s.letap = letap.data();
-    s.lzetam = lzetam.data(); s.lzetap = lzetap.data(); s.elemBC = bc.data();
-    s.symm = symm.data();
-    s.prm = {1e-7, 1e-7, 1e-7, 1e-10, 1e-7, r.hg, 4.0 / 3.0, 1e12, 1.0, 2.0, 0.5, 2.0 / 3.0, 2.0,
-             1e9, 1e-9, 0.0, -1e15, 0.1, 1.0};
-
-    // reverse neighbour map (as lg_adjoint.cu builds it)
-    vector<int> revStart(E + 1, 0), revEntry;
-    {
-        vector<vector<int>> lists(E);
-        const vector<int> *nb[6] = {&lxim, &lxip, &letam, &letap, &lzetam, &lzetap};
-        const int mm[3] = {XI_M, ETA_M, ZETA_M}, ms[3] = {XI_M_SYMM, ETA_M_SYMM, ZETA_M_SYMM},
-                  mf[3] = {XI_M_FREE, ETA_M_FREE, ZETA_M_FREE};
-        const int pm[3] = {XI_P, ETA_P, ZETA_P}, ps[3] = {XI_P_SYMM, ETA_P_SYMM, ZETA_P_SYMM},
-                  pf[3] = {XI_P_FREE, ETA_P_FREE, ZETA_P_FREE};
-        auto uses = [](int bits, int mask, int sym, int fr) {
-            const int b = bits & mask;
-            return b == 0 || (b != sym && b != fr && b == (mask & ~(sym | fr)));
-        };
-        for (int j = 0; j < E; ++j)
-            for (int dd = 0; dd < 3; ++dd) {
-                if (uses(bc[j], mm[dd], ms[dd], mf[dd])) lists[(*nb[2 * dd])[j]].push_back(j * 6 + 2 * dd);
-                if (uses(bc[j], pm[dd], ps[dd], pf[dd])) lists[(*nb[2 * dd + 1])[j]].push_back(j * 6 + 2 * dd + 1);
-            }
-        for (int k = 0; k < E; ++k) {
-            revStart[k + 1] = revStart[k] + (int)lists[k].size();
-            revEntry.insert(revEntry.end(), lists[k].begin(), lists[k].end());
-        }
-    }
-
-    // adjoint arrays
-    vector<double> nbar(6 * (size_t)N, 0.), ebar(5 * (size_t)E, 0.), vnewb(E), dxb(3 * (size_t)E),
-        dvb(3 * (size_t)E), slot(6 * (size_t)E), corner(48 * (size_t)E), fb(3 * (size_t)N), hgpart(1);
+    hostadj::Tape tape(d, r.ncyc);
+    hostadj::Adjoint adj(d, r.hg);
     for (int i = 0; i < E; ++i)
-        if (r.mask[i]) ebar[i] = volo[i];
-    adj::AdjArgs A;
-    for (int i = 0; i < 6; ++i) A.nb[i] = &nbar[(size_t)i * N];
-    A.eb = &ebar[0]; A.pb = &ebar[E]; A.qb = &ebar[2 * (size_t)E]; A.vb = &ebar[3 * (size_t)E];
-    A.ssb = &ebar[4 * (size_t)E];
-    A.vnewb = vnewb.data();
-    for (int i = 0; i < 3; ++i) {
-        A.delxb[i] = &dxb[(size_t)i * E];
-        A.delvb[i] = &dvb[(size_t)i * E];
-    }
-    A.slot = slot.data(); A.corner = corner.data(); A.fb = fb.data(); A.hgPart = hgpart.data();
-    A.revStart = revStart.data(); A.revEntry = revEntry.data(); A.hg = r.hg;
-    auto snap_at = [&](int c) {
-        adj::Snap sn;
-        double *b = &snaps[c * snapD];
-        for (int i = 0; i < 6; ++i) sn.n[i] = b + (size_t)i * N;
-        for (int i = 0; i < 5; ++i) sn.el[i] = b + 6 * (size_t)N + (size_t)i * E;
-        return sn;
-    };
-    double hgb = 0.;
-    for (int c = r.ncyc - 1; c >= 0; --c) {
-        A.s0 = snap_at(c);
-        A.s1 = snap_at(c + 1);
-        for (int t = 0; t < 8; ++t) A.tc.t[t] = &temps[(c * 8 + t) * (size_t)E];
-        A.dt = r.dts[c];
-        for (int k = 0; k < E; ++k) adj::adj_material(s, A, k);
-        for (int k = 0; k < E; ++k) adj::adj_qslots(s, A, k);
-        for (int k = 0; k < E; ++k) adj::adj_kinematics(s, A, k);
-        for (int n = 0; n < N; ++n) adj::adj_nodes(s, A, n);
-        for (int k = 0; k < E; ++k) hgb += adj::adj_forces(s, A, k);
-        for (int n = 0; n < N; ++n) adj::adj_gather(s, A, n);
-    }
+        if (r.mask[i]) adj.ebar[i] = adj.volo[i];
+    const double hgb = adj.backward(tape, r.dts.data());
+    const vector<double> &ebar = adj.ebar;
 
     // finite differences
     double worst = 0.;
