@@ -128,6 +128,8 @@ __device__ __forceinline__ R monoq_phi(R limiter_mult, R max_slope, const R *dv,
 // and ordinary comparisons.  lg_fastmath.cuh has the mixed path's variant
 // with the same interface.
 struct IeeeOps {
+    // ssc_of skips the square root for warps whose lanes all take the floor
+    static constexpr bool kWarpSkip = true;
     static __device__ __forceinline__ double div(double a, double b) { return a / b; }
     static __device__ __forceinline__ double sqrt_(double a) { return sqrt(a); }
     static __device__ __forceinline__ bool lt(double a, double b) { return a < b; }
@@ -141,6 +143,18 @@ template <class M = IeeeOps>
 __device__ __forceinline__ double ssc_of(double num, double rho0)
 {
     double ssc = (rho0 == 1.0) ? num : M::div(num, rho0);
+    if constexpr (M::kWarpSkip) {
+        // Elements at rest take the floor.  A predicated square root would
+        // still occupy the FP64 pipe for a warp of them, so the sequence
+        // runs only when a converged lane of the warp needs it.
+        const bool floor = M::le(ssc, .1111111e-36);
+        double r = .3333333e-18;
+        if (__any_sync(__activemask(), !floor)) {
+            const double t = M::sqrt_(floor ? 1.0 : ssc);
+            if (!floor) r = t;
+        }
+        return r;
+    }
     if (M::le(ssc, .1111111e-36))
         ssc = .3333333e-18;
     else

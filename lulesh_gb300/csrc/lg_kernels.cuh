@@ -404,16 +404,19 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
     }
     if (MODE != 0) {
         // CalcCourantConstraintForElems (2447-2513) and
-        // CalcHydroConstraintForElems (2517-2572) for one element
-        const double qqc2 = 64.0 * P.qqc * P.qqc;
-        const double ssv = s.ss[ielem];
+        // CalcHydroConstraintForElems (2517-2572) for one element.  The
+        // reference evaluates the Courant dt of every element but keeps it
+        // only where vdov != 0; a warp of elements at rest skips it.
         const double vdov = s.vdov[ielem];
-        const double arealg = s.arealg[ielem];
-        double dtf = ssv * ssv;
-        if (vdov < 0.) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
-        dtf = sqrt(dtf);
-        dtf = arealg / dtf;
-        if (vdov != 0.) {
+        const bool moving = vdov != 0.;
+        if (__any_sync(__activemask(), moving) && moving) {
+            const double qqc2 = 64.0 * P.qqc * P.qqc;
+            const double ssv = s.ss[ielem];
+            const double arealg = s.arealg[ielem];
+            double dtf = ssv * ssv;
+            if (vdov < 0.) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
+            dtf = sqrt(dtf);
+            dtf = arealg / dtf;
             if (dtf < dtc) dtc = dtf;
             const double dtdvov = P.dvovmax / (fabs(vdov) + 1.e-20);
             if (dth > dtdvov) dth = dtdvov;

@@ -392,14 +392,17 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
         s.v[ielem] = tmpV;
     }
     if (MODE != 0) {
-        const double qqc2 = 64.0 * P.qqc * P.qqc;
-        const double ssv = s.ss[ielem];
+        // Only elements with vdov != 0 constrain dt; a warp of elements at
+        // rest skips the FP64 square root and reciprocals altogether.
         const double vdov = s.vdov[ielem];
-        const double arealg = s.arealg[ielem];
-        double dtf = ssv * ssv;
-        if (FastOps::lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
-        dtf = arealg * rcp_nr(sqrt_nr(dtf));
-        if (vdov != 0.) {
+        const bool moving = ((unsigned long long)__double_as_longlong(vdov) << 1) != 0ull;
+        if (__any_sync(__activemask(), moving) && moving) {
+            const double qqc2 = 64.0 * P.qqc * P.qqc;
+            const double ssv = s.ss[ielem];
+            const double arealg = s.arealg[ielem];
+            double dtf = ssv * ssv;
+            if (FastOps::lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
+            dtf = arealg * rcp_nr(sqrt_nr(dtf));
             if (dtf < dtc) dtc = dtf;
             const double dtdvov = P.dvovmax * rcp_nr(fabs(vdov) + 1.e-20);
             if (dth > dtdvov) dth = dtdvov;
