@@ -140,7 +140,9 @@ int upload_inv_mass(lg_domain *d, const double *m, size_t n)
 }
 
 // regNumList and the region-ordered element permutation with each
-// position's EOS repetition count, from the host region sets.
+// position's EOS repetition count, from the host region sets.  Regions are
+// visited most repetitions first (lg::region_visit_order); each region's
+// elements keep their ascending regElemlist order.
 int upload_regions(lg_domain *d)
 {
     const lg::Problem &p = d->prob;
@@ -148,7 +150,7 @@ int upload_regions(lg_domain *d)
     std::vector<int> perm, rep;
     perm.reserve(E);
     rep.reserve(E);
-    for (int r = 0; r < p.numReg; ++r) {
+    for (const int r : lg::region_visit_order(p.numReg, p.cost)) {
         const int rr = lg::region_rep(r, p.numReg, p.cost);
         for (int e : p.regElemlist[r]) {
             perm.push_back(e);

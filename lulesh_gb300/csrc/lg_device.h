@@ -12,9 +12,9 @@
 //                       delv_* buffers);
 //   symm[n]             bit 0/1/2 set when node n is in symmX/Y/Z;
 //   regPerm[t], regRep[t]  region-sorted element order and the EOS
-//                       repetition count of position t (regions in order,
-//                       ascending element ids inside each region, the order
-//                       of regElemlist).
+//                       repetition count of position t (regions with the
+//                       most repetitions first, ascending element ids inside
+//                       each region, the order of regElemlist).
 #pragma once
 
 #include <cstdint>

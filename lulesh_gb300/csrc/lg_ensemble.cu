@@ -259,7 +259,8 @@ int setup_members(lg_ensemble *en, bool topology)
 }
 
 // region order over all members (global element ids, each member's regions
-// in turn) with the EOS repetition counts, and the members' hgcoef
+// in turn, most EOS repetitions first as in lg::region_visit_order) with the
+// EOS repetition counts, and the members' hgcoef
 int upload_regions(lg_ensemble *en)
 {
     const long long E = en->E;
@@ -270,7 +271,7 @@ int upload_regions(lg_ensemble *en)
         const lg::Problem &p = en->prob[pi];
         const long long eo = en->eoff[pi];
         hg[pi] = p.k.hgcoef;
-        for (int r = 0; r < p.numReg; ++r) {
+        for (const int r : lg::region_visit_order(p.numReg, p.cost)) {
             const int rr = lg::region_rep(r, p.numReg, p.cost);
             for (int e : p.regElemlist[r]) {
                 perm[pos] = (int)(e + eo);

@@ -1,6 +1,8 @@
 // lg_problem.cc -- host-side Sedov problem set-up and the end-of-run report.
 #include "lg_problem.h"
 
+#include <algorithm>
+
 #include <cmath>
 #include <cstdio>
 #include <sstream>
@@ -74,6 +76,16 @@ int region_rep(int r, int numReg, int cost)
     if (r < numReg / 2) return 1;
     if (r < (numReg - (numReg + 15) / 20)) return 1 + cost;
     return 10 * (1 + cost);
+}
+
+std::vector<int> region_visit_order(int numReg, int cost)
+{
+    std::vector<int> order(numReg);
+    for (int r = 0; r < numReg; ++r) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return region_rep(a, numReg, cost) > region_rep(b, numReg, cost);
+    });
+    return order;
 }
 
 void build_corner_list(Problem &p)

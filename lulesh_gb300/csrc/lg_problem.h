@@ -91,6 +91,13 @@ double elem_volume_host(const double x[8], const double y[8], const double z[8])
 // EOS repetitions of region r, lulesh.cc:2390-2400.
 int region_rep(int r, int numReg, int cost);
 
+// The order in which the material kernels visit the regions: most EOS
+// repetitions first, ascending region index among equals.  Every element's
+// material update is independent and the dt reduction is a minimum, so the
+// order cannot change a result; putting the expensive blocks at the front of
+// the grid keeps them from forming a tail that leaves SMs idle.
+std::vector<int> region_visit_order(int numReg, int cost);
+
 // End-of-run report text, lulesh-util.cc:175-230.
 std::string format_report(int nx, int cycle, double e0, double maxAbsDiff,
                           double totalAbsDiff, double maxRelDiff, double elapsed);
