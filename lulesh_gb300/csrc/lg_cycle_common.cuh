@@ -85,6 +85,34 @@ __device__ __forceinline__ bool cycle_live(const Ctl *c) { return c->active && c
 // k_material
 // ---------------------------------------------------------------------------
 
+// Exact comparisons of doubles on the integer pipe.  On GB300 an FP64
+// comparison occupies the FP64 pipe like an FMA, and the FP64 pipe bounds
+// every FP64 kernel here.  The results equal IEEE comparisons for operands
+// that are not NaN (the cycle stops on a volume error before a NaN can
+// form).  dkey() maps a double to a signed integer of the same order, with
+// -0 and +0 both at 0 since they compare equal.
+__device__ __forceinline__ long long dkey(double v)
+{
+    const long long b = __double_as_longlong(v);
+    const long long sgn = b >> 63;  // 0 or -1
+    return (b ^ (sgn & 0x7fffffffffffffffLL)) - sgn;
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return dkey(a) < dkey(b); }
+__device__ __forceinline__ bool dle(double a, double b) { return dkey(a) <= dkey(b); }
+// |a| < b for b >= +0: the magnitude bits order like the magnitudes
+__device__ __forceinline__ bool dabs_lt(double a, double b)
+{
+    return (__double_as_longlong(a) & 0x7fffffffffffffffLL) < __double_as_longlong(b);
+}
+// a != 0 (true for NaN, as in IEEE)
+__device__ __forceinline__ bool dnz(double a)
+{
+    return ((unsigned long long)__double_as_longlong(a) << 1) != 0ull;
+}
+// a < b in the arithmetic type of the limiter
+__device__ __forceinline__ bool less(float a, float b) { return a < b; }
+__device__ __forceinline__ bool less(double a, double b) { return dlt(a, b); }
+
 // one direction of CalcMonotonicQRegionForElems, lulesh.cc:1778-1813
 template <typename R>
 __device__ __forceinline__ R monoq_phi(R limiter_mult, R max_slope, const R *dv, int ielem, int bc,
@@ -117,10 +145,10 @@ __device__ __forceinline__ R monoq_phi(R limiter_mult, R max_slope, const R *dv,
     R phi = R(.5) * (delvm + delvp);
     delvm *= limiter_mult;
     delvp *= limiter_mult;
-    if (delvm < phi) phi = delvm;
-    if (delvp < phi) phi = delvp;
-    if (phi < R(0.)) phi = R(0.);
-    if (phi > max_slope) phi = max_slope;
+    if (less(delvm, phi)) phi = delvm;
+    if (less(delvp, phi)) phi = delvp;
+    if (less(phi, R(0.))) phi = R(0.);
+    if (less(max_slope, phi)) phi = max_slope;
     return phi;
 }
 
@@ -136,6 +164,14 @@ struct IeeeOps {
     static __device__ __forceinline__ bool le(double a, double b) { return a <= b; }
     // |a| < b
     static __device__ __forceinline__ bool abs_lt(double a, double b) { return fabs(a) < b; }
+};
+
+// IEEE division and square root with the comparisons on the integer pipe
+// (dlt, dle, dabs_lt): the operations of the FP64 builds' EOS.
+struct IntCmpOps : IeeeOps {
+    static __device__ __forceinline__ bool lt(double a, double b) { return dlt(a, b); }
+    static __device__ __forceinline__ bool le(double a, double b) { return dle(a, b); }
+    static __device__ __forceinline__ bool abs_lt(double a, double b) { return dabs_lt(a, b); }
 };
 
 // sound-speed term of lulesh.cc:2083-2090, 2126-2133, 2158-2165, 2190-2197

@@ -36,6 +36,9 @@
 #ifndef LG_NS
 #error "define LG_NS"
 #endif
+#ifndef LG_EOS_OPS
+#define LG_EOS_OPS IntCmpOps
+#endif
 
 namespace lg {
 namespace LG_NS {
@@ -192,11 +195,11 @@ __device__ __forceinline__ void nodes_node(const DevState &s, const int n, const
     const double dt = ctl->deltatime;
     const double u_cut = s.prm.u_cut;
     double xd = s.xd[n] + xdd * dt;
-    if (fabs(xd) < u_cut) xd = 0.0;
+    if (dabs_lt(xd, u_cut)) xd = 0.0;
     double yd = s.yd[n] + ydd * dt;
-    if (fabs(yd) < u_cut) yd = 0.0;
+    if (dabs_lt(yd, u_cut)) yd = 0.0;
     double zd = s.zd[n] + zdd * dt;
-    if (fabs(zd) < u_cut) zd = 0.0;
+    if (dabs_lt(zd, u_cut)) zd = 0.0;
     s.xd[n] = xd;
     s.yd[n] = yd;
     s.zd[n] = zd;
@@ -354,16 +357,16 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
         const double vnew = s.vnew[ielem];
         const double vdov = s.vdov[ielem];
         double qlin, qquad;
-        if (vdov > 0.) {
+        if (dlt(0., vdov)) {
             qlin = 0.;
             qquad = 0.;
         } else {
             double delvxxi = s.delv_xi[ielem] * s.delx_xi[ielem];
             double delvxeta = s.delv_eta[ielem] * s.delx_eta[ielem];
             double delvxzeta = s.delv_zeta[ielem] * s.delx_zeta[ielem];
-            if (delvxxi > 0.) delvxxi = 0.;
-            if (delvxeta > 0.) delvxeta = 0.;
-            if (delvxzeta > 0.) delvxzeta = 0.;
+            if (dlt(0., delvxxi)) delvxxi = 0.;
+            if (dlt(0., delvxeta)) delvxeta = 0.;
+            if (dlt(0., delvxzeta)) delvxzeta = 0.;
             const double rho = s.elemMass[ielem] / (s.volo[ielem] * vnew);
             qlin = -P.qlc_monoq * rho *
                    (delvxxi * (1. - phixi) + delvxeta * (1. - phieta) +
@@ -378,19 +381,19 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
 
         // qstop check on the previous cycle's q, lulesh.cc:1993-2008
         const double q_old = s.q[ielem];
-        if (q_old > P.qstop) ctl->err_qstop = 1;
+        if (dlt(P.qstop, q_old)) ctl->err_qstop = 1;
 
         // ApplyMaterialPropertiesForElems, lulesh.cc:2328-2406
         double vnewc = vnew;
-        if (P.eosvmin != 0. && vnewc < P.eosvmin) vnewc = P.eosvmin;
-        if (P.eosvmax != 0. && vnewc > P.eosvmax) vnewc = P.eosvmax;
+        if (dnz(P.eosvmin) && dlt(vnewc, P.eosvmin)) vnewc = P.eosvmin;
+        if (dnz(P.eosvmax) && dlt(P.eosvmax, vnewc)) vnewc = P.eosvmax;
         double vc = s.v[ielem];
-        if (P.eosvmin != 0. && vc < P.eosvmin) vc = P.eosvmin;
-        if (P.eosvmax != 0. && vc > P.eosvmax) vc = P.eosvmax;
-        if (vc <= 0.) ctl->err_matvol = 1;
+        if (dnz(P.eosvmin) && dlt(vc, P.eosvmin)) vc = P.eosvmin;
+        if (dnz(P.eosvmax) && dlt(P.eosvmax, vc)) vc = P.eosvmax;
+        if (dle(vc, 0.)) ctl->err_matvol = 1;
 
         double p_new, e_new, q_new, ss_new;
-        eval_eos(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin, vnewc,
+        eval_eos<LG_EOS_OPS>(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin, vnewc,
                  s.regRep[t], p_new, e_new, q_new, ss_new);
         s.p[ielem] = p_new;
         s.e[ielem] = e_new;
@@ -399,7 +402,7 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
 
         // UpdateVolumesForElems, lulesh.cc:2410-2427
         double tmpV = vnew;
-        if (fabs(tmpV - 1.0) < P.v_cut) tmpV = 1.0;
+        if (dabs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
         s.v[ielem] = tmpV;
     }
     if (MODE != 0) {
@@ -408,18 +411,18 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
         // reference evaluates the Courant dt of every element but keeps it
         // only where vdov != 0; a warp of elements at rest skips it.
         const double vdov = s.vdov[ielem];
-        const bool moving = vdov != 0.;
+        const bool moving = dnz(vdov);
         if (__any_sync(__activemask(), moving) && moving) {
             const double qqc2 = 64.0 * P.qqc * P.qqc;
             const double ssv = s.ss[ielem];
             const double arealg = s.arealg[ielem];
             double dtf = ssv * ssv;
-            if (vdov < 0.) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
+            if (dlt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
             dtf = sqrt(dtf);
             dtf = arealg / dtf;
-            if (dtf < dtc) dtc = dtf;
+            if (dlt(dtf, dtc)) dtc = dtf;
             const double dtdvov = P.dvovmax / (fabs(vdov) + 1.e-20);
-            if (dth > dtdvov) dth = dtdvov;
+            if (dlt(dtdvov, dth)) dth = dtdvov;
         }
     }
 }
