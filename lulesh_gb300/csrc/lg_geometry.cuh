@@ -16,27 +16,47 @@ using std::sqrt;
 namespace lg {
 namespace geom {
 
+// a < b.  Device code compares doubles through an order-preserving integer
+// key (-0 and +0 equal), which equals the IEEE comparison for non-NaN
+// operands and keeps it off GB300's FP64 pipe.
+template <typename R>
+LG_HD bool lt(R a, R b)
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(R) == 8) {
+        const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
+        const long long sa = ba >> 63, sb = bb >> 63;
+        return ((ba ^ (sa & 0x7fffffffffffffffLL)) - sa) < ((bb ^ (sb & 0x7fffffffffffffffLL)) - sb);
+    }
+#endif
+    return a < b;
+}
+
 // ---------------------------------------------------------------------------
 // element geometry (lulesh.cc:290-474, 591-663, 1273-1435)
 // ---------------------------------------------------------------------------
 
-// Jacobian determinant of CalcElemShapeFunctionDerivatives (lulesh.cc:319-376)
+// Jacobian determinant of CalcElemShapeFunctionDerivatives (lulesh.cc:319-376).
+// The reference scales each of the nine sums by 0.125 and the triple
+// product by 8; those powers of two combine to one factor 2^-6.  Scaling by a
+// power of two is exact, so the value is the reference's bit for bit (for
+// coordinates far from the underflow range).
 template <typename R>
 LG_HD R jacobian_det(const R *x, const R *y, const R *z)
 {
-    const R fjxxi = R(.125) * ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
-    const R fjxet = R(.125) * ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
-    const R fjxze = R(.125) * ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
-    const R fjyxi = R(.125) * ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
-    const R fjyet = R(.125) * ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
-    const R fjyze = R(.125) * ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
-    const R fjzxi = R(.125) * ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
-    const R fjzet = R(.125) * ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
-    const R fjzze = R(.125) * ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
+    const R fjxxi = ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxet = ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxze = ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
+    const R fjyxi = ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyet = ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyze = ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
+    const R fjzxi = ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzet = ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzze = ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
     const R cjxet = -(fjyxi * fjzze) + (fjzxi * fjyze);
     const R cjyet = (fjxxi * fjzze) - (fjzxi * fjxze);
     const R cjzet = -(fjxxi * fjyze) + (fjyxi * fjxze);
-    return R(8.) * (fjxet * cjxet + fjyet * cjyet + fjzet * cjzet);
+    return R(0.015625) * (fjxet * cjxet + fjyet * cjyet + fjzet * cjzet);
 }
 
 // CalcElemShapeFunctionDerivatives rows 0..3 of B (rows 4..7 are their
@@ -78,20 +98,73 @@ LG_HD R shape_derivs(const R *x, const R *y, const R *z, R bx[4], R by[4],
     return R(8.) * (fjxet * cjxet + fjyet * cjyet + fjzet * cjzet);
 }
 
-// SumElemFaceNormal, lulesh.cc:381-415 (the four corners a,b,c,d of a face)
+// shape_derivs without the reference's power-of-two factors: returns 64 x the
+// determinant and fills 64 x rows 0..3 of B.  A velocity gradient formed as
+// (1 / det) * (B . v) from these equals the one formed from shape_derivs bit
+// for bit, since only powers of two were dropped and they cancel exactly.
+template <typename R>
+LG_HD R shape_derivs_x64(const R *x, const R *y, const R *z, R bx[4], R by[4], R bz[4])
+{
+    const R fjxxi = ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxet = ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxze = ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
+    const R fjyxi = ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyet = ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyze = ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
+    const R fjzxi = ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzet = ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzze = ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
+    const R cjxxi = (fjyet * fjzze) - (fjzet * fjyze);
+    const R cjxet = -(fjyxi * fjzze) + (fjzxi * fjyze);
+    const R cjxze = (fjyxi * fjzet) - (fjzxi * fjyet);
+    const R cjyxi = -(fjxet * fjzze) + (fjzet * fjxze);
+    const R cjyet = (fjxxi * fjzze) - (fjzxi * fjxze);
+    const R cjyze = -(fjxxi * fjzet) + (fjzxi * fjxet);
+    const R cjzxi = (fjxet * fjyze) - (fjyet * fjxze);
+    const R cjzet = -(fjxxi * fjyze) + (fjyxi * fjxze);
+    const R cjzze = (fjxxi * fjyet) - (fjyxi * fjxet);
+    bx[0] = -cjxxi - cjxet - cjxze;
+    bx[1] = cjxxi - cjxet - cjxze;
+    bx[2] = cjxxi + cjxet - cjxze;
+    bx[3] = -cjxxi + cjxet - cjxze;
+    by[0] = -cjyxi - cjyet - cjyze;
+    by[1] = cjyxi - cjyet - cjyze;
+    by[2] = cjyxi + cjyet - cjyze;
+    by[3] = -cjyxi + cjyet - cjyze;
+    bz[0] = -cjzxi - cjzet - cjzze;
+    bz[1] = cjzxi - cjzet - cjzze;
+    bz[2] = cjzxi + cjzet - cjzze;
+    bz[3] = -cjzxi + cjzet - cjzze;
+    return fjxet * cjxet + fjyet * cjyet + fjzet * cjzet;
+}
+
+// Area vector of SumElemFaceNormal, lulesh.cc:381-415 (the four corners
+// a,b,c,d of a face).  Twice the reference's bisectors are formed; its
+// factors 0.5 (each bisector) and 0.25 (the area) are applied once as
+// 0.0625.  Powers of two scale exactly, so the area vector is the
+// reference's bit for bit.
+template <typename R>
+LG_HD void face_area(const R *x, const R *y, const R *z, int a, int b, int c, int d, R &areaX,
+                     R &areaY, R &areaZ)
+{
+    const R bisectX0 = (x[d] + x[c] - x[b] - x[a]);
+    const R bisectY0 = (y[d] + y[c] - y[b] - y[a]);
+    const R bisectZ0 = (z[d] + z[c] - z[b] - z[a]);
+    const R bisectX1 = (x[c] + x[b] - x[d] - x[a]);
+    const R bisectY1 = (y[c] + y[b] - y[d] - y[a]);
+    const R bisectZ1 = (z[c] + z[b] - z[d] - z[a]);
+    areaX = R(0.0625) * (bisectY0 * bisectZ1 - bisectZ0 * bisectY1);
+    areaY = R(0.0625) * (bisectZ0 * bisectX1 - bisectX0 * bisectZ1);
+    areaZ = R(0.0625) * (bisectX0 * bisectY1 - bisectY0 * bisectX1);
+}
+
+// SumElemFaceNormal, lulesh.cc:381-415
 template <typename R>
 LG_HD void face_normal(R *nx, R *ny, R *nz, const R *x, const R *y,
                                             const R *z, int a, int b, int c, int d)
 {
-    const R bisectX0 = R(0.5) * (x[d] + x[c] - x[b] - x[a]);
-    const R bisectY0 = R(0.5) * (y[d] + y[c] - y[b] - y[a]);
-    const R bisectZ0 = R(0.5) * (z[d] + z[c] - z[b] - z[a]);
-    const R bisectX1 = R(0.5) * (x[c] + x[b] - x[d] - x[a]);
-    const R bisectY1 = R(0.5) * (y[c] + y[b] - y[d] - y[a]);
-    const R bisectZ1 = R(0.5) * (z[c] + z[b] - z[d] - z[a]);
-    const R areaX = R(0.25) * (bisectY0 * bisectZ1 - bisectZ0 * bisectY1);
-    const R areaY = R(0.25) * (bisectZ0 * bisectX1 - bisectX0 * bisectZ1);
-    const R areaZ = R(0.25) * (bisectX0 * bisectY1 - bisectY0 * bisectX1);
+    R areaX, areaY, areaZ;
+    face_area(x, y, z, a, b, c, d, areaX, areaY, areaZ);
     nx[a] += areaX; nx[b] += areaX; nx[c] += areaX; nx[d] += areaX;
     ny[a] += areaY; ny[b] += areaY; ny[c] += areaY; ny[d] += areaY;
     nz[a] += areaZ; nz[b] += areaZ; nz[c] += areaZ; nz[d] += areaZ;
@@ -112,9 +185,57 @@ LG_HD void node_normals(R *pfx, R *pfy, R *pfz, const R *x, const R *y,
     face_normal(pfx, pfy, pfz, x, y, z, 4, 7, 6, 5);
 }
 
+// CalcElemNodeNormals with each node's three face areas summed in the
+// reference's face order but starting from the first area instead of from
+// 0.0.  Equal to node_normals except for the sign of an all-zero sum; the
+// FMA build uses it (the strict build keeps node_normals).
+template <typename R>
+LG_HD void node_normals_nozero(R *pfx, R *pfy, R *pfz, const R *x, const R *y, const R *z)
+{
+    R ax[6], ay[6], az[6];
+    constexpr int F[6][4] = {{0, 1, 2, 3}, {0, 4, 5, 1}, {1, 5, 6, 2},
+                             {2, 6, 7, 3}, {3, 7, 4, 0}, {4, 7, 6, 5}};
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+        face_area(x, y, z, F[f][0], F[f][1], F[f][2], F[f][3], ax[f], ay[f], az[f]);
+    // faces of node n, in face order: 0:{0,1,4} 1:{0,1,2} 2:{0,2,3} 3:{0,3,4}
+    // 4:{1,4,5} 5:{1,2,5} 6:{2,3,5} 7:{3,4,5}
+#define LG_NN(P, A)                                 \
+    P[0] = (A[0] + A[1]) + A[4];                    \
+    P[1] = (A[0] + A[1]) + A[2];                    \
+    P[2] = (A[0] + A[2]) + A[3];                    \
+    P[3] = (A[0] + A[3]) + A[4];                    \
+    P[4] = (A[1] + A[4]) + A[5];                    \
+    P[5] = (A[1] + A[2]) + A[5];                    \
+    P[6] = (A[2] + A[3]) + A[5];                    \
+    P[7] = (A[3] + A[4]) + A[5];
+    LG_NN(pfx, ax)
+    LG_NN(pfy, ay)
+    LG_NN(pfz, az)
+#undef LG_NN
+}
+
+// The four hourglass mode sums sum_k gam(m, k) * v[k] of CalcFBHourglassForceForElems
+// (lulesh.cc:894-920) by a pairwise butterfly: 18 additions instead of 28.
+// The FMA build uses it; it rounds differently from the left-to-right sums.
+template <typename R>
+LG_HD void hourglass_modes(const R *v, R m[4])
+{
+    const R s01 = v[0] + v[1], d01 = v[0] - v[1];
+    const R s23 = v[2] + v[3], d23 = v[2] - v[3];
+    const R s45 = v[4] + v[5], d45 = v[4] - v[5];
+    const R s67 = v[6] + v[7], d67 = v[6] - v[7];
+    const R a = d01 + d67, b = d23 + d45;
+    m[0] = (s01 + s67) - (s23 + s45);
+    m[1] = a - b;
+    m[2] = a + b;
+    m[3] = (d45 + d67) - (d01 + d23);
+}
+
 // VoluDer, lulesh.cc:591-619, for corner k of CalcElemVolumeDerivative
 // (lulesh.cc:623-663) with neighbour nodes m0..m5
-template <typename R>
+// (kScale = false leaves out the final factor 1/12: 12 x dV/dx)
+template <typename R, bool kScale = true>
 LG_HD void volu_der(const R *x, const R *y, const R *z, int m0, int m1, int m2,
                                          int m3, int m4, int m5, R &dvdx, R &dvdy, R &dvdz)
 {
@@ -128,23 +249,25 @@ LG_HD void volu_der(const R *x, const R *y, const R *z, int m0, int m1, int m2,
            (x3 + x4) * (z0 + z4) + (x2 + x5) * (z3 + z5) - (x3 + x5) * (z2 + z5);
     dvdz = -(y1 + y2) * (x0 + x1) + (y0 + y1) * (x1 + x2) - (y0 + y4) * (x3 + x4) +
            (y3 + y4) * (x0 + x4) + (y2 + y5) * (x3 + x5) - (y3 + y5) * (x2 + x5);
-    dvdx *= twelfth;
-    dvdy *= twelfth;
-    dvdz *= twelfth;
+    if (kScale) {
+        dvdx *= twelfth;
+        dvdy *= twelfth;
+        dvdz *= twelfth;
+    }
 }
 
-template <typename R>
+template <typename R, bool kScale = true>
 LG_HD void volume_derivative(const R *x, const R *y, const R *z, R *dvdx,
                                                   R *dvdy, R *dvdz)
 {
-    volu_der(x, y, z, 1, 2, 3, 4, 5, 7, dvdx[0], dvdy[0], dvdz[0]);
-    volu_der(x, y, z, 0, 1, 2, 7, 4, 6, dvdx[3], dvdy[3], dvdz[3]);
-    volu_der(x, y, z, 3, 0, 1, 6, 7, 5, dvdx[2], dvdy[2], dvdz[2]);
-    volu_der(x, y, z, 2, 3, 0, 5, 6, 4, dvdx[1], dvdy[1], dvdz[1]);
-    volu_der(x, y, z, 7, 6, 5, 0, 3, 1, dvdx[4], dvdy[4], dvdz[4]);
-    volu_der(x, y, z, 4, 7, 6, 1, 0, 2, dvdx[5], dvdy[5], dvdz[5]);
-    volu_der(x, y, z, 5, 4, 7, 2, 1, 3, dvdx[6], dvdy[6], dvdz[6]);
-    volu_der(x, y, z, 6, 5, 4, 3, 2, 0, dvdx[7], dvdy[7], dvdz[7]);
+    volu_der<R, kScale>(x, y, z, 1, 2, 3, 4, 5, 7, dvdx[0], dvdy[0], dvdz[0]);
+    volu_der<R, kScale>(x, y, z, 0, 1, 2, 7, 4, 6, dvdx[3], dvdy[3], dvdz[3]);
+    volu_der<R, kScale>(x, y, z, 3, 0, 1, 6, 7, 5, dvdx[2], dvdy[2], dvdz[2]);
+    volu_der<R, kScale>(x, y, z, 2, 3, 0, 5, 6, 4, dvdx[1], dvdy[1], dvdz[1]);
+    volu_der<R, kScale>(x, y, z, 7, 6, 5, 0, 3, 1, dvdx[4], dvdy[4], dvdz[4]);
+    volu_der<R, kScale>(x, y, z, 4, 7, 6, 1, 0, 2, dvdx[5], dvdy[5], dvdz[5]);
+    volu_der<R, kScale>(x, y, z, 5, 4, 7, 2, 1, 3, dvdx[6], dvdy[6], dvdz[6]);
+    volu_der<R, kScale>(x, y, z, 6, 5, 4, 3, 2, 0, dvdx[7], dvdy[7], dvdz[7]);
 }
 
 // CalcElemVolume, lulesh.cc:1273-1356
@@ -197,13 +320,80 @@ template <typename R>
 LG_HD R char_length(const R *x, const R *y, const R *z, R volume)
 {
     R cl = R(0.0), a;
-    a = area_face(x, y, z, 0, 1, 2, 3); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 4, 5, 6, 7); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 0, 1, 5, 4); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 1, 2, 6, 5); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 2, 3, 7, 6); cl = (a < cl) ? cl : a;
-    a = area_face(x, y, z, 3, 0, 4, 7); cl = (a < cl) ? cl : a;
+    a = area_face(x, y, z, 0, 1, 2, 3); cl = lt(a, cl) ? cl : a;
+    a = area_face(x, y, z, 4, 5, 6, 7); cl = lt(a, cl) ? cl : a;
+    a = area_face(x, y, z, 0, 1, 5, 4); cl = lt(a, cl) ? cl : a;
+    a = area_face(x, y, z, 1, 2, 6, 5); cl = lt(a, cl) ? cl : a;
+    a = area_face(x, y, z, 2, 3, 7, 6); cl = lt(a, cl) ? cl : a;
+    a = area_face(x, y, z, 3, 0, 4, 7); cl = lt(a, cl) ? cl : a;
     return R(4.0) * volume / sqrt(cl);
+}
+
+// CalcMonotonicQGradientsForElems for one element (lulesh.cc:1613-1757):
+// out = {delx_xi, delx_eta, delx_zeta, delv_xi, delv_eta, delv_zeta}.
+// kFold drops the reference's factors 0.25 on the eighteen coordinate and
+// velocity differences and compensates with exact powers of two (16 on the
+// length numerator with 256 x ptiny under the root, 1/64 on norm): without
+// contraction every output is the reference's bit for bit.  kFold = false is
+// the reference's formulation.
+template <typename R, bool kFold>
+LG_HD void monoq_gradients(const R *x, const R *y, const R *z, const R *xv, const R *yv,
+                           const R *zv, R vol, R out[6])
+{
+    const R q = kFold ? R(1) : R(.25);
+    const R ptiny_s = kFold ? R(256.e-36) : R(1.e-36);
+    const R norm = kFold ? (R(1.0) / (vol + R(1.e-36))) * R(0.015625) : R(1.0) / (vol + R(1.e-36));
+    const R vol_s = kFold ? R(16.0) * vol : vol;
+#define S4(A, a, b, c, d) (A[a] + A[b] + A[c] + A[d])
+#define SC(e) (kFold ? (e) : q * (e))
+    const R dxj = SC(-(S4(x, 0, 1, 5, 4) - S4(x, 3, 2, 6, 7)));
+    const R dyj = SC(-(S4(y, 0, 1, 5, 4) - S4(y, 3, 2, 6, 7)));
+    const R dzj = SC(-(S4(z, 0, 1, 5, 4) - S4(z, 3, 2, 6, 7)));
+    const R dxi = SC((S4(x, 1, 2, 6, 5) - S4(x, 0, 3, 7, 4)));
+    const R dyi = SC((S4(y, 1, 2, 6, 5) - S4(y, 0, 3, 7, 4)));
+    const R dzi = SC((S4(z, 1, 2, 6, 5) - S4(z, 0, 3, 7, 4)));
+    const R dxk = SC((S4(x, 4, 5, 6, 7) - S4(x, 0, 1, 2, 3)));
+    const R dyk = SC((S4(y, 4, 5, 6, 7) - S4(y, 0, 1, 2, 3)));
+    const R dzk = SC((S4(z, 4, 5, 6, 7) - S4(z, 0, 1, 2, 3)));
+    R ax, ay, az, dxv, dyv, dzv;
+
+    ax = dyi * dzj - dzi * dyj;
+    ay = dzi * dxj - dxi * dzj;
+    az = dxi * dyj - dyi * dxj;
+    out[2] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
+    ax *= norm;
+    ay *= norm;
+    az *= norm;
+    dxv = SC((S4(xv, 4, 5, 6, 7) - S4(xv, 0, 1, 2, 3)));
+    dyv = SC((S4(yv, 4, 5, 6, 7) - S4(yv, 0, 1, 2, 3)));
+    dzv = SC((S4(zv, 4, 5, 6, 7) - S4(zv, 0, 1, 2, 3)));
+    out[5] = ax * dxv + ay * dyv + az * dzv;
+
+    ax = dyj * dzk - dzj * dyk;
+    ay = dzj * dxk - dxj * dzk;
+    az = dxj * dyk - dyj * dxk;
+    out[0] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
+    ax *= norm;
+    ay *= norm;
+    az *= norm;
+    dxv = SC((S4(xv, 1, 2, 6, 5) - S4(xv, 0, 3, 7, 4)));
+    dyv = SC((S4(yv, 1, 2, 6, 5) - S4(yv, 0, 3, 7, 4)));
+    dzv = SC((S4(zv, 1, 2, 6, 5) - S4(zv, 0, 3, 7, 4)));
+    out[3] = ax * dxv + ay * dyv + az * dzv;
+
+    ax = dyk * dzi - dzk * dyi;
+    ay = dzk * dxi - dxk * dzi;
+    az = dxk * dyi - dyk * dxi;
+    out[1] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
+    ax *= norm;
+    ay *= norm;
+    az *= norm;
+    dxv = SC(-(S4(xv, 0, 1, 5, 4) - S4(xv, 3, 2, 6, 7)));
+    dyv = SC(-(S4(yv, 0, 1, 5, 4) - S4(yv, 3, 2, 6, 7)));
+    dzv = SC(-(S4(zv, 0, 1, 5, 4) - S4(zv, 3, 2, 6, 7)));
+    out[4] = ax * dxv + ay * dyv + az * dzv;
+#undef SC
+#undef S4
 }
 
 // hourglass base vectors, lulesh.cc:743-776

@@ -39,6 +39,15 @@
 #ifndef LG_EOS_OPS
 #define LG_EOS_OPS IntCmpOps
 #endif
+// LG_REASSOC (the FMA build): the hourglass and node-normal sums are
+// regrouped to save FP64 instructions (node_normals_nozero, the
+// hourglass_modes butterfly, and the 1/12 and 1/volume factors applied once
+// per mode instead of once per term).  The rounding differs from the
+// reference's operand order, as FMA contraction's does; the parity bar
+// covers both.
+#ifndef LG_REASSOC
+#define LG_REASSOC 0
+#endif
 
 namespace lg {
 namespace LG_NS {
@@ -73,7 +82,11 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
         const double sig = -s.p[k] - s.q[k];
         const double determ = jacobian_det(x, y, z);
         double pfx[8], pfy[8], pfz[8];
+#if LG_REASSOC
+        node_normals_nozero(pfx, pfy, pfz, x, y, z);
+#else
         node_normals(pfx, pfy, pfz, x, y, z);
+#endif
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             cs[0 * E8 + (size_t)j * E + k] = -(sig * pfx[j]);
@@ -91,6 +104,26 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
 
     // CalcFBHourglassForceForElems (710-991), CalcElemFBHourglassForce (667-706)
     double hourgam[8][4];
+#if LG_REASSOC
+    {
+        // 12 x dV/dx, with 1/(12 volume) folded into the four mode sums
+        double dvdx[8], dvdy[8], dvdz[8];
+        volume_derivative<double, false>(x, y, z, dvdx, dvdy, dvdz);
+        const double volinv12 = (1.0 / determ) * (1.0 / 12.0);
+        double hmx[4], hmy[4], hmz[4];
+        hourglass_modes(x, hmx);
+        hourglass_modes(y, hmy);
+        hourglass_modes(z, hmz);
+#pragma unroll
+        for (int i1 = 0; i1 < 4; ++i1) {
+            const double hx = volinv12 * hmx[i1], hy = volinv12 * hmy[i1],
+                         hz = volinv12 * hmz[i1];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                hourgam[kk][i1] = gam(i1, kk) - dvdx[kk] * hx - dvdy[kk] * hy - dvdz[kk] * hz;
+        }
+    }
+#else
     {
         double dvdx[8], dvdy[8], dvdz[8];
         volume_derivative(x, y, z, dvdx, dvdy, dvdz);
@@ -113,6 +146,7 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
                                                           dvdz[kk] * hourmodz);
         }
     }
+#endif
     const double ss1 = s.ss[k];
     const double mass1 = s.elemMass[k];
     const double volume13 = cbrt(determ);
@@ -256,9 +290,16 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
             yh[j] = y[j] - dt2 * yv[j];
             zh[j] = z[j] - dt2 * zv[j];
         }
+        // Strict build: 64 x the determinant and 64 x B, whose factors cancel
+        // exactly in inv_detJ * (B . v).  The FMA build keeps the reference's
+        // formulation: with contraction the two are not bitwise equal, and
+        // its parity margin was measured with this one.
         double bx[4], by[4], bz[4];
-        const double detJ = shape_derivs(xh, yh, zh, bx, by, bz);
-        const double inv_detJ = 1.0 / detJ;
+#if LG_REASSOC
+        const double inv_detJ = 1.0 / shape_derivs(xh, yh, zh, bx, by, bz);
+#else
+        const double inv_detJ = 1.0 / shape_derivs_x64(xh, yh, zh, bx, by, bz);
+#endif
         const double dxx = inv_detJ * (bx[0] * (xv[0] - xv[6]) + bx[1] * (xv[1] - xv[7]) +
                                        bx[2] * (xv[2] - xv[4]) + bx[3] * (xv[3] - xv[5]));
         const double dyy = inv_detJ * (by[0] * (yv[0] - yv[6]) + by[1] * (yv[1] - yv[7]) +
@@ -270,57 +311,14 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
     if (relativeVolume <= 0.0) raise_status(ctl, -1);  // lulesh.cc:1598-1605
 
     // CalcMonotonicQGradientsForElems
-    const double ptiny = 1.e-36;
-    double ax, ay, az, dxv, dyv, dzv;
-    const double vol = volo * relativeVolume;
-    const double norm = 1.0 / (vol + ptiny);
-#define S4(A, a, b, c, d) (A[a] + A[b] + A[c] + A[d])
-    const double dxj = -0.25 * (S4(x, 0, 1, 5, 4) - S4(x, 3, 2, 6, 7));
-    const double dyj = -0.25 * (S4(y, 0, 1, 5, 4) - S4(y, 3, 2, 6, 7));
-    const double dzj = -0.25 * (S4(z, 0, 1, 5, 4) - S4(z, 3, 2, 6, 7));
-    const double dxi = 0.25 * (S4(x, 1, 2, 6, 5) - S4(x, 0, 3, 7, 4));
-    const double dyi = 0.25 * (S4(y, 1, 2, 6, 5) - S4(y, 0, 3, 7, 4));
-    const double dzi = 0.25 * (S4(z, 1, 2, 6, 5) - S4(z, 0, 3, 7, 4));
-    const double dxk = 0.25 * (S4(x, 4, 5, 6, 7) - S4(x, 0, 1, 2, 3));
-    const double dyk = 0.25 * (S4(y, 4, 5, 6, 7) - S4(y, 0, 1, 2, 3));
-    const double dzk = 0.25 * (S4(z, 4, 5, 6, 7) - S4(z, 0, 1, 2, 3));
-
-    ax = dyi * dzj - dzi * dyj;
-    ay = dzi * dxj - dxi * dzj;
-    az = dxi * dyj - dyi * dxj;
-    s.delx_zeta[k] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
-    ax *= norm;
-    ay *= norm;
-    az *= norm;
-    dxv = 0.25 * (S4(xv, 4, 5, 6, 7) - S4(xv, 0, 1, 2, 3));
-    dyv = 0.25 * (S4(yv, 4, 5, 6, 7) - S4(yv, 0, 1, 2, 3));
-    dzv = 0.25 * (S4(zv, 4, 5, 6, 7) - S4(zv, 0, 1, 2, 3));
-    s.delv_zeta[k] = ax * dxv + ay * dyv + az * dzv;
-
-    ax = dyj * dzk - dzj * dyk;
-    ay = dzj * dxk - dxj * dzk;
-    az = dxj * dyk - dyj * dxk;
-    s.delx_xi[k] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
-    ax *= norm;
-    ay *= norm;
-    az *= norm;
-    dxv = 0.25 * (S4(xv, 1, 2, 6, 5) - S4(xv, 0, 3, 7, 4));
-    dyv = 0.25 * (S4(yv, 1, 2, 6, 5) - S4(yv, 0, 3, 7, 4));
-    dzv = 0.25 * (S4(zv, 1, 2, 6, 5) - S4(zv, 0, 3, 7, 4));
-    s.delv_xi[k] = ax * dxv + ay * dyv + az * dzv;
-
-    ax = dyk * dzi - dzk * dyi;
-    ay = dzk * dxi - dxk * dzi;
-    az = dxk * dyi - dyk * dxi;
-    s.delx_eta[k] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
-    ax *= norm;
-    ay *= norm;
-    az *= norm;
-    dxv = -0.25 * (S4(xv, 0, 1, 5, 4) - S4(xv, 3, 2, 6, 7));
-    dyv = -0.25 * (S4(yv, 0, 1, 5, 4) - S4(yv, 3, 2, 6, 7));
-    dzv = -0.25 * (S4(zv, 0, 1, 5, 4) - S4(zv, 3, 2, 6, 7));
-    s.delv_eta[k] = ax * dxv + ay * dyv + az * dzv;
-#undef S4
+    double g[6];
+    monoq_gradients<double, !LG_REASSOC>(x, y, z, xv, yv, zv, volo * relativeVolume, g);
+    s.delx_xi[k] = g[0];
+    s.delx_eta[k] = g[1];
+    s.delx_zeta[k] = g[2];
+    s.delv_xi[k] = g[3];
+    s.delv_eta[k] = g[4];
+    s.delv_zeta[k] = g[5];
 }
 
 template <bool BATCHED, int BS>
