@@ -63,28 +63,33 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 
 
 # FP64 thread-instructions (DADD + DMUL + DFMA) per element per launch,
-# from an ncu capture of each kernel of the strict and the FMA build at
-# s=100, 11 regions (k_nodes: counted per node, stored per element at
-# s=100's N/E; k_material: the s=100 region mix); absent where not measured.
+# from an ncu capture of the four cycle kernels at cycle 170 of the
+# reference problem: s=100, 11 regions for the strict and the FMA builds;
+# s=96, 16 regions, balance 2, cost 4 for the mixed build (k_nodes: counted
+# per node, stored per element at that mesh's N/E; k_material: that region
+# mix).
 FP64_INST_PER_ELEM = {
-    "fp64": {"k_forces": 1363, "k_kinematics": 728, "k_material": 770,
-             "k_nodes": 113 * 1030301 / 1000000},
-    "fp64-fma": {"k_forces": 955, "k_kinematics": 606, "k_material": 729,
+    "fp64": {"k_forces": 1321, "k_kinematics": 699, "k_material": 783,
+             "k_nodes": 115.6 * 1030301 / 1000000},
+    "fp64-fma": {"k_forces": 828, "k_kinematics": 601, "k_material": 724,
                  "k_nodes": 109.6 * 1030301 / 1000000},
+    "mixed": {"k_forces": 22, "k_kinematics": 94, "k_material": 576,
+              "k_nodes": 12.0 * 912673 / 884736},
 }
+# The region mix (regions, balance, cost) each build's k_material count was
+# taken with; the EOS repetitions make that count depend on it.
+FP64_INST_REGION_MIX = {"fp64": (11, 1, 1), "fp64-fma": (11, 1, 1), "mixed": (16, 2, 4)}
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element per
-# launch (k_nodes: per node), from one ncu capture of each kernel on a smaller
-# mesh of the same problem, scaled to the benchmarked mesh by the units it
-# processes: s=100 for the FP64 builds, s=96 r16 b2 c4 for the mixed one.
-# Well above the algorithmic bytes: the per-corner force
-# scratch (k_forces writes, k_nodes reads) and the region-order gathers of
-# k_material.
+# launch (k_nodes: per node), from the same ncu captures, scaled to the
+# benchmarked mesh by the units it processes.  Well above the algorithmic
+# bytes: the per-corner force scratch (k_forces writes, k_nodes reads) and
+# the region-order gathers of k_material.
 TRAFFIC_PER_UNIT = {
-    "fp64": {"k_forces": 456.3, "k_nodes": 540.0, "k_kinematics": 140.1, "k_material": 224.3},
-    "fp64-fma": {"k_forces": 456.1, "k_nodes": 553.5, "k_kinematics": 138.9, "k_material": 220.1},
-    "mixed": {"k_forces": 264.7, "k_nodes": 338.2, "k_kinematics": 120.8, "k_material": 174.4},
+    "fp64": {"k_forces": 457.2, "k_nodes": 540.2, "k_kinematics": 140.4, "k_material": 210.8},
+    "fp64-fma": {"k_forces": 456.2, "k_nodes": 539.9, "k_kinematics": 140.8, "k_material": 210.7},
+    "mixed": {"k_forces": 264.4, "k_nodes": 337.7, "k_kinematics": 120.6, "k_material": 162.6},
 }
 
 
@@ -442,6 +447,9 @@ def run_gpu(a):
     # FP64 pipe roofline (the bound of this path)
     fp64_peak = lg.measure_pipe("fma")
     per_elem = FP64_INST_PER_ELEM.get(a.precision, {}).get(dom)
+    if dom == "k_material" and FP64_INST_REGION_MIX.get(a.precision) != (a.regions, a.balance,
+                                                                         a.cost):
+        per_elem = None  # counted with another region mix
     roof64 = {"bound": "fp64_pipe", "peak_ginst_per_s": fp64_peak, "unit": "G FP64 inst/s",
               "kernel": dom}
     if per_elem:
