@@ -1,7 +1,11 @@
 // lg_geometry.cuh -- hex-element geometry of the reference, generic in the
 // arithmetic type (double for the FP64 paths, float for the FP32 parts of the
-// mixed path).  Every expression keeps the reference's operand order; with
-// R = double the code is the reference's arithmetic operation for operation.
+// mixed path).  Every expression keeps the reference's operand order.  Where
+// the reference scales by powers of two, some functions apply the product of
+// those factors once (each says so); a power of two scales a rounded result
+// exactly, so with R = double and no contraction the values are the
+// reference's bit for bit.  node_normals_nozero and hourglass_modes regroup
+// sums and round differently; only the FMA build uses them.
 #pragma once
 
 #ifdef __CUDACC__

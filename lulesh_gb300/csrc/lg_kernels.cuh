@@ -19,11 +19,16 @@
 //                 cycle's TimeIncrement
 //
 // Every arithmetic expression keeps the reference's operand order (see the
-// oracle's lulesh_oracle.c for the line-by-line correspondence).  Work the
-// reference does and then discards (the shape-function B matrix that
-// CalcElemNodeNormals overwrites, the off-diagonal velocity gradient terms,
-// the deviatoric strains) is not computed; division by refdens is skipped
-// when refdens == 1 (x / 1.0 == x exactly).
+// oracle's lulesh_oracle.c for the line-by-line correspondence), with two
+// kinds of exception.  Exact ones, in both builds: power-of-two factors
+// applied once (lg_geometry.cuh) and comparisons of doubles on the integer
+// pipe (dlt and friends); the strict build's results stay those of the
+// reference's operation order bit for bit.  Rounding ones, in the FMA build
+// only: the regrouped sums under LG_REASSOC.  Work the reference does and
+// then discards (the shape-function B matrix that CalcElemNodeNormals
+// overwrites, the off-diagonal velocity gradient terms, the deviatoric
+// strains, the Courant dt of elements with vdov == 0) is not computed;
+// division by refdens is skipped when refdens == 1 (x / 1.0 == x exactly).
 #pragma once
 
 #include <cuda_runtime.h>
