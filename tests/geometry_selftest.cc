@@ -1,0 +1,130 @@
+// geometry_selftest.cc -- the element geometry of lg_geometry.cuh, compiled
+// for the host without contraction, against the oracle's functions
+// (geometry_ref_shim.c) on random hexahedra.  Where lg_geometry.cuh applies
+// the reference's power-of-two factors once (face areas, Jacobian, the
+// half-step B matrix and the monotonic-Q gradients), the results must be
+// the same bits.  Prints the number of mismatches; exits 1 if any.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+#include "lg_geometry.cuh"
+#include "lulesh_oracle.h"
+
+extern "C" {
+void geo_ref_shape(const double *x, const double *y, const double *z, double *b24, double *det);
+void geo_ref_normals(const double *x, const double *y, const double *z, double *pfx, double *pfy,
+                     double *pfz);
+void geo_ref_volume_derivative(const double *x, const double *y, const double *z, double *dvdx,
+                               double *dvdy, double *dvdz);
+double geo_ref_volume(const double *x, const double *y, const double *z);
+double geo_ref_char_length(const double *x, const double *y, const double *z, double volume);
+void geo_ref_monoq_gradients(orc_domain *d);
+}
+
+using namespace lg::geom;
+
+static bool same(double a, double b) { return std::memcmp(&a, &b, sizeof a) == 0; }
+
+static long g_bad = 0;
+static void check(const char *what, double want, double got)
+{
+    if (!same(want, got)) {
+        if (g_bad < 10) std::printf("mismatch %s: %.17g vs %.17g\n", what, want, got);
+        ++g_bad;
+    }
+}
+
+// one half of the kinematics' velocity-gradient trace: inv_detJ * (B . dv)
+static double grad(double inv, const double *b, const double *v)
+{
+    return inv * (b[0] * (v[0] - v[6]) + b[1] * (v[1] - v[7]) + b[2] * (v[2] - v[4]) +
+                  b[3] * (v[3] - v[5]));
+}
+
+int main(int argc, char **argv)
+{
+    const long n = argc > 1 ? std::atol(argv[1]) : 200000;
+    std::mt19937_64 g(12345);
+    std::uniform_real_distribution<double> u(-1.0, 1.0), sc(1e-4, 10.0);
+    const double cx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1},
+                 cz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    for (long it = 0; it < n; ++it) {
+        const double h = sc(g), jit = (it % 3 == 0) ? 0.4 : (it % 3 == 1 ? 1e-3 : 0.0);
+        const double o[3] = {10 * u(g), 10 * u(g), 10 * u(g)};
+        double x[8], y[8], z[8], xv[8], yv[8], zv[8];
+        for (int j = 0; j < 8; ++j) {
+            x[j] = o[0] + h * (cx[j] + jit * u(g));
+            y[j] = o[1] + h * (cy[j] + jit * u(g));
+            z[j] = o[2] + h * (cz[j] + jit * u(g));
+            xv[j] = u(g);
+            yv[j] = u(g);
+            zv[j] = u(g);
+        }
+        double b[24], det;
+        geo_ref_shape(x, y, z, b, &det);
+        check("jacobian_det", det, jacobian_det(x, y, z));
+        double bx[4], by[4], bz[4];
+        const double inv = 1.0 / det, inv64 = 1.0 / shape_derivs_x64(x, y, z, bx, by, bz);
+        check("dxx", grad(inv, b, xv), grad(inv64, bx, xv));
+        check("dyy", grad(inv, b + 8, yv), grad(inv64, by, yv));
+        check("dzz", grad(inv, b + 16, zv), grad(inv64, bz, zv));
+        double rx[8], ry[8], rz[8], px[8], py[8], pz[8];
+        geo_ref_normals(x, y, z, rx, ry, rz);
+        node_normals(px, py, pz, x, y, z);
+        for (int j = 0; j < 8; ++j) {
+            check("normal x", rx[j], px[j]);
+            check("normal y", ry[j], py[j]);
+            check("normal z", rz[j], pz[j]);
+        }
+        geo_ref_volume_derivative(x, y, z, rx, ry, rz);
+        volume_derivative(x, y, z, px, py, pz);
+        for (int j = 0; j < 8; ++j) {
+            check("dvdx", rx[j], px[j]);
+            check("dvdy", ry[j], py[j]);
+            check("dvdz", rz[j], pz[j]);
+        }
+        const double vol = geo_ref_volume(x, y, z);
+        check("volume", vol, elem_volume(x, y, z));
+        check("char_length", geo_ref_char_length(x, y, z, vol), char_length(x, y, z, vol));
+    }
+
+    // monotonic-Q gradients: the oracle's domain-level loop on a jittered
+    // mesh with random velocities and relative volumes
+    orc_domain *d = orc_create(6, 11, 1, 1);
+    size_t N = 0, E = 0, L = 0;
+    double *X = orc_field_f64(d, "x", &N), *Y = orc_field_f64(d, "y", nullptr),
+           *Z = orc_field_f64(d, "z", nullptr), *XD = orc_field_f64(d, "xd", nullptr),
+           *YD = orc_field_f64(d, "yd", nullptr), *ZD = orc_field_f64(d, "zd", nullptr);
+    double *vnew = orc_field_f64(d, "vnew", &E), *volo = orc_field_f64(d, "volo", nullptr);
+    const int *nl = orc_field_i32(d, "nodelist", &L);
+    for (size_t i = 0; i < N; ++i) {
+        X[i] += 0.02 * u(g);
+        Y[i] += 0.02 * u(g);
+        Z[i] += 0.02 * u(g);
+        XD[i] = u(g);
+        YD[i] = u(g);
+        ZD[i] = u(g);
+    }
+    for (size_t k = 0; k < E; ++k) vnew[k] = 1.0 + 0.3 * u(g);
+    geo_ref_monoq_gradients(d);
+    const char *names[6] = {"delx_xi", "delx_eta", "delx_zeta", "delv_xi", "delv_eta", "delv_zeta"};
+    const double *want[6];
+    for (int c = 0; c < 6; ++c) want[c] = orc_field_f64(d, names[c], nullptr);
+    for (size_t k = 0; k < E; ++k) {
+        double x[8], y[8], z[8], xv[8], yv[8], zv[8], out[6];
+        for (int j = 0; j < 8; ++j) {
+            const int m = nl[8 * k + j];
+            x[j] = X[m]; y[j] = Y[m]; z[j] = Z[m];
+            xv[j] = XD[m]; yv[j] = YD[m]; zv[j] = ZD[m];
+        }
+        monoq_gradients<double, true>(x, y, z, xv, yv, zv, volo[k] * vnew[k], out);
+        for (int c = 0; c < 6; ++c) check(names[c], want[c][k], out[c]);
+        monoq_gradients<double, false>(x, y, z, xv, yv, zv, volo[k] * vnew[k], out);
+        for (int c = 0; c < 6; ++c) check(names[c], want[c][k], out[c]);
+    }
+    orc_destroy(d);
+    std::printf("%ld random elements, %zu mesh elements, mismatches %ld\n", n, E, g_bad);
+    return g_bad != 0;
+}
