@@ -152,25 +152,16 @@ __device__ __forceinline__ R monoq_phi(R limiter_mult, R max_slope, const R *dv,
     return phi;
 }
 
-// The reference's FP64 arithmetic for the EOS: IEEE division and square root
-// and ordinary comparisons.  lg_fastmath.cuh has the mixed path's variant
-// with the same interface.
+// The FP64 builds' arithmetic for the EOS: IEEE division and square root, and
+// comparisons on the integer pipe (dlt, dle, dabs_lt; the IEEE results for
+// every non-NaN operand).  lg_fastmath.cuh has the mixed path's variant with
+// the same interface.
 struct IeeeOps {
-    // ssc_of skips the square root for warps whose lanes all take the floor
-    static constexpr bool kWarpSkip = true;
     static __device__ __forceinline__ double div(double a, double b) { return a / b; }
     static __device__ __forceinline__ double sqrt_(double a) { return sqrt(a); }
-    static __device__ __forceinline__ bool lt(double a, double b) { return a < b; }
-    static __device__ __forceinline__ bool le(double a, double b) { return a <= b; }
-    // |a| < b
-    static __device__ __forceinline__ bool abs_lt(double a, double b) { return fabs(a) < b; }
-};
-
-// IEEE division and square root with the comparisons on the integer pipe
-// (dlt, dle, dabs_lt): the operations of the FP64 builds' EOS.
-struct IntCmpOps : IeeeOps {
     static __device__ __forceinline__ bool lt(double a, double b) { return dlt(a, b); }
     static __device__ __forceinline__ bool le(double a, double b) { return dle(a, b); }
+    // |a| < b for b >= +0
     static __device__ __forceinline__ bool abs_lt(double a, double b) { return dabs_lt(a, b); }
 };
 
@@ -178,24 +169,17 @@ struct IntCmpOps : IeeeOps {
 template <class M = IeeeOps>
 __device__ __forceinline__ double ssc_of(double num, double rho0)
 {
-    double ssc = (rho0 == 1.0) ? num : M::div(num, rho0);
-    if constexpr (M::kWarpSkip) {
-        // Elements at rest take the floor.  A predicated square root would
-        // still occupy the FP64 pipe for a warp of them, so the sequence
-        // runs only when a converged lane of the warp needs it.
-        const bool floor = M::le(ssc, .1111111e-36);
-        double r = .3333333e-18;
-        if (__any_sync(__activemask(), !floor)) {
-            const double t = M::sqrt_(floor ? 1.0 : ssc);
-            if (!floor) r = t;
-        }
-        return r;
+    const double ssc = (rho0 == 1.0) ? num : M::div(num, rho0);
+    // Elements at rest take the floor.  A predicated square root would still
+    // occupy the FP64 pipe for a warp of them, so the sequence runs only when
+    // a converged lane of the warp needs it.
+    const bool floor = M::le(ssc, .1111111e-36);
+    double r = .3333333e-18;
+    if (__any_sync(__activemask(), !floor)) {
+        const double t = M::sqrt_(floor ? 1.0 : ssc);
+        if (!floor) r = t;
     }
-    if (M::le(ssc, .1111111e-36))
-        ssc = .3333333e-18;
-    else
-        ssc = M::sqrt_(ssc);
-    return ssc;
+    return r;
 }
 
 // CalcPressureForElems for one element, lulesh.cc:2014-2044

@@ -92,8 +92,6 @@ __device__ __forceinline__ unsigned long long order_key(double v)
 
 // FP64 EOS operations of the mixed path (same interface as IeeeOps)
 struct FastOps {
-    // ssc_of skips the square root for warps whose lanes all take the floor
-    static constexpr bool kWarpSkip = true;
     static __device__ __forceinline__ double div(double a, double b) { return a * rcp_nr(b); }
     static __device__ __forceinline__ double sqrt_(double a) { return sqrt_nr(a); }
     static __device__ __forceinline__ bool lt(double a, double b) { return order_key(a) < order_key(b); }

@@ -41,9 +41,6 @@
 #ifndef LG_NS
 #error "define LG_NS"
 #endif
-#ifndef LG_EOS_OPS
-#define LG_EOS_OPS IntCmpOps
-#endif
 // LG_REASSOC (the FMA build): the hourglass and node-normal sums are
 // regrouped to save FP64 instructions (node_normals_nozero, the
 // hourglass_modes butterfly, and the 1/12 and 1/volume factors applied once
@@ -396,7 +393,7 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
         if (dle(vc, 0.)) ctl->err_matvol = 1;
 
         double p_new, e_new, q_new, ss_new;
-        eval_eos<LG_EOS_OPS>(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin, vnewc,
+        eval_eos(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin, vnewc,
                  s.regRep[t], p_new, e_new, q_new, ss_new);
         s.p[ielem] = p_new;
         s.e[ielem] = e_new;
