@@ -64,7 +64,7 @@ struct DevState {
     int E, N, nx, numReg;
     // node fields
     double *x, *y, *z, *xd, *yd, *zd, *xdd, *ydd, *zdd, *fx, *fy, *fz, *nodalMass;
-    double *invMass;  // 1 / nodalMass (mixed path)
+    double *invMass;  // RN(1 / nodalMass): the nodal accelerations of every path
     uint8_t *symm;
     int *nodeElemStart, *nodeElemCornerList;
     // element fields

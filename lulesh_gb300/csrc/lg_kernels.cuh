@@ -185,6 +185,20 @@ __global__ void __launch_bounds__(BS) k_forces(DevState s)
     }
 }
 
+// f / m, rounded as the IEEE quotient, from rm = RN(1 / m) (the set-up's
+// invMass, constant over the run) by Markstein's residual correction
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990): q0 = RN(f rm), the exact
+// residual f - m q0 by one FMA, q = RN(q0 + residual rm).  Three FP64
+// instructions instead of a division; equal to f / m for operands in the
+// normal range whose residual does not underflow.  An exact q0 (zero
+// residual) is returned as is, which keeps the sign of a zero quotient.
+__device__ __forceinline__ double div_by_mass(double f, double m, double rm)
+{
+    const double q0 = __dmul_rn(f, rm);
+    const double res = __fma_rn(-m, q0, f);
+    return dnz(res) ? __fma_rn(res, rm, q0) : q0;
+}
+
 // ---------------------------------------------------------------------------
 // k_nodes: corner gather (lulesh.cc:565-582, 969-986), CalcAccelerationForNodes
 // (1139-1149), ApplyAccelerationBoundaryConditionsForNodes (1153-1179),
@@ -219,8 +233,9 @@ __device__ __forceinline__ void nodes_node(const DevState &s, const int n, const
     s.fx[n] = fx;
     s.fy[n] = fy;
     s.fz[n] = fz;
-    const double m = s.nodalMass[n];
-    double xdd = fx / m, ydd = fy / m, zdd = fz / m;
+    const double m = s.nodalMass[n], rm = s.invMass[n];
+    double xdd = div_by_mass(fx, m, rm), ydd = div_by_mass(fy, m, rm),
+           zdd = div_by_mass(fz, m, rm);
     const int sym = s.symm[n];
     if (sym & 1) xdd = 0.0;
     if (sym & 2) ydd = 0.0;

@@ -1,4 +1,4 @@
-"""Host checks of two exactness claims the FP64 kernels rest on.
+"""Host checks of the exactness claims the FP64 kernels rest on.
 
 1. lg_geometry.cuh applies the reference's power-of-two factors once (face
    areas, Jacobian, half-step B matrix, monotonic-Q gradients).  Compiled for
@@ -10,6 +10,9 @@
    key = (b ^ (sign & 0x7fff...)) - sign, sign = b >> 63.  Restated here in
    int64 arithmetic, it must order every non-NaN double as IEEE comparison
    does, with -0 equal to +0.
+3. The nodal acceleration f / m is formed from the constant RN(1/m) by
+   Markstein's residual correction (div_by_mass in lg_kernels.cuh); restated
+   in division_selftest.cc, it must equal the IEEE quotient.
 """
 import os
 import shutil
@@ -67,3 +70,14 @@ def test_integer_key_orders_doubles_like_ieee():
     mag = np.abs(a).view(np.int64)
     for c in cuts:
         assert np.array_equal(mag < np.float64(c).view(np.int64), np.abs(a) < c)
+
+
+def test_mass_quotient_equals_ieee_division(tmp_path):
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    exe = tmp_path / "division_selftest"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                    os.path.join(ROOT, "tests", "division_selftest.cc"), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe), "20000000"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:]
+    assert r.stdout.strip().endswith("mismatches 0"), r.stdout[-2000:]
