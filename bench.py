@@ -70,9 +70,9 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 # mix).
 FP64_INST_PER_ELEM = {
     "fp64": {"k_forces": 1321, "k_kinematics": 699, "k_material": 783,
-             "k_nodes": 115.6 * 1030301 / 1000000},
+             "k_nodes": 73.6 * 1030301 / 1000000},
     "fp64-fma": {"k_forces": 828, "k_kinematics": 601, "k_material": 724,
-                 "k_nodes": 109.6 * 1030301 / 1000000},
+                 "k_nodes": 67.6 * 1030301 / 1000000},
     "mixed": {"k_forces": 22, "k_kinematics": 94, "k_material": 576,
               "k_nodes": 12.0 * 912673 / 884736},
 }
@@ -87,8 +87,8 @@ FP64_INST_REGION_MIX = {"fp64": (11, 1, 1), "fp64-fma": (11, 1, 1), "mixed": (16
 # bytes: the per-corner force scratch (k_forces writes, k_nodes reads) and
 # the region-order gathers of k_material.
 TRAFFIC_PER_UNIT = {
-    "fp64": {"k_forces": 457.2, "k_nodes": 540.2, "k_kinematics": 140.4, "k_material": 210.8},
-    "fp64-fma": {"k_forces": 456.2, "k_nodes": 539.9, "k_kinematics": 140.8, "k_material": 210.7},
+    "fp64": {"k_forces": 456.8, "k_nodes": 550.9, "k_kinematics": 140.3, "k_material": 210.5},
+    "fp64-fma": {"k_forces": 456.2, "k_nodes": 550.3, "k_kinematics": 140.4, "k_material": 210.9},
     "mixed": {"k_forces": 264.4, "k_nodes": 337.7, "k_kinematics": 120.6, "k_material": 162.6},
 }
 
