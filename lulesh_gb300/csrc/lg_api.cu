@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "lg_device.h"
@@ -77,6 +78,9 @@ struct lg_domain {
     cudaGraphExec_t graph1 = nullptr, graph16 = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int its = 9999999;
+    // k_material's work items: threads one wave of it keeps resident, and the
+    // capacity of regPerm / regRep (upload_regions)
+    int resident = 0, item_cap = 0;
     bool host_only = false;  // device < 0: problem set-up only, no GPU
     long long launches = 0;  // kernels queued by this handle
     // frozen / recorded time steps (lg_dt_freeze, lg_dt_record)
@@ -139,29 +143,66 @@ int upload_inv_mass(lg_domain *d, const double *m, size_t n)
     return upload(d, d->ds.invMass, inv);
 }
 
-// regNumList and the region-ordered element permutation with each
-// position's EOS repetition count, from the host region sets.  Regions are
-// visited most repetitions first (lg::region_visit_order); each region's
-// elements keep their ascending regElemlist order.
+// regNumList and k_material's work items (DevState::nItems) from the host
+// region sets: elements in region order, the regions with the most EOS
+// repetitions first (lg::region_visit_order), each region's elements in their
+// ascending regElemlist order, each item with its repetition count.
+//
+// On a small mesh the costly regions fill too few blocks to keep every SM's
+// FP64 pipe busy: at s=30 the 10(1+cost)-repetition elements make 35 blocks
+// for 152 SMs, which run their repetitions one after another while the other
+// SMs idle.  There (FP64 builds) the elements of each repetition count whose
+// elements number fewer than T (three blocks of 128 per SM) get f items that
+// share their repetitions, f = min(ceil(T / count), rep, 32).  All items of
+// an element sit in one block of 128 (padding where a group would straddle
+// two), so the kernel's barrier orders every item's reads before the
+// writer's stores.  The work done and the results are unchanged.
 int upload_regions(lg_domain *d)
 {
     const lg::Problem &p = d->prob;
     const int E = p.numElem;
+    const std::vector<int> order = lg::region_visit_order(p.numReg, p.cost);
+    // elements per repetition count
+    std::map<int, long long> count;
+    for (int r = 0; r < p.numReg; ++r)
+        count[lg::region_rep(r, p.numReg, p.cost)] += (long long)p.regElemlist[r].size();
+    const long long T = 3LL * d->resident / 8;
+    const bool split = d->opts.precision != LG_MIXED;
+    auto items_of = [&](int rr) -> int {
+        const long long n = count[rr];
+        if (!split || rr < 2 || n >= T || n == 0) return 1;
+        return (int)std::min<long long>({(T + n - 1) / n, (long long)rr, 32LL});
+    };
     std::vector<int> perm, rep;
     perm.reserve(E);
     rep.reserve(E);
-    for (const int r : lg::region_visit_order(p.numReg, p.cost)) {
+    int writers = 0;
+    for (const int r : order) {
         const int rr = lg::region_rep(r, p.numReg, p.cost);
+        const int f = items_of(rr);
         for (int e : p.regElemlist[r]) {
-            perm.push_back(e);
-            rep.push_back(rr);
+            if (f > 1 && (int)(perm.size() % 128) + f > 128)
+                while (perm.size() % 128) {
+                    perm.push_back(-1);
+                    rep.push_back(0);
+                }
+            for (int i = 0; i < f; ++i) {
+                const int share = rr / f + (i < rr % f ? 1 : 0);
+                perm.push_back(e);
+                rep.push_back(i == f - 1 ? share : -share);
+            }
+            ++writers;
         }
     }
-    if ((int)perm.size() != E) return set_error(LG_ERR_INVALID, "region sets do not cover all elements");
+    if (writers != E) return set_error(LG_ERR_INVALID, "region sets do not cover all elements");
+    if ((long long)perm.size() > d->item_cap)
+        return set_error(LG_ERR_STATE, "%zu work items exceed the capacity %d", perm.size(),
+                         d->item_cap);
     int st;
     if ((st = upload(d, d->ds.regNumList, p.regNumList))) return st;
     if ((st = upload(d, d->ds.regPerm, perm))) return st;
     if ((st = upload(d, d->ds.regRep, rep))) return st;
+    d->ds.nItems = (int)perm.size();
     LG_CUDA(cudaStreamSynchronize(d->stream));
     return LG_OK;
 }
@@ -482,7 +523,15 @@ int lg_create(const lg_opts *opts, lg_domain **out)
         return LG_OK;
     }
     const size_t E = p.numElem, N = p.numNode;
-    const int eblocks = (int)((E + 127) / 128);
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opts->device) != cudaSuccess ||
+        sms < 1)
+        sms = 1;
+    d->resident = sms * 8 * 128;  // 8 blocks of 128 threads per SM (64 registers)
+    // upload_regions adds at most T = 3/8 resident items for each of the two
+    // split repetition counts, plus padding of at most 31 in 128
+    d->item_cap = (int)(E + 2 * (size_t)d->resident);
+    const int eblocks = (int)((d->item_cap + 127) / 128);
 
     Layout L;
     size_t o_node[14], o_elem[19];
@@ -492,7 +541,8 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     const size_t o_nl = L.add<int>(8 * E), o_nlT = L.add<int>(8 * E);
     size_t o_conn[7];
     for (auto &o : o_conn) o = L.add<int>(E);
-    const size_t o_regnum = L.add<int>(E), o_perm = L.add<int>(E), o_rep = L.add<int>(E);
+    const size_t o_regnum = L.add<int>(E), o_perm = L.add<int>(d->item_cap),
+                 o_rep = L.add<int>(d->item_cap);
     const size_t o_nes = L.add<int>(N + 1), o_ncl = L.add<int>(8 * E);
     const size_t o_symm = L.add<uint8_t>(N);
     const size_t o_part = L.add<double>(2 * (size_t)eblocks);
@@ -508,6 +558,7 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     lg::DevState &s = d->ds;
     s.E = (int)E;
     s.N = (int)N;
+    s.nItems = (int)E;
     s.nx = p.nx;
     s.numReg = p.numReg;
     double **nodef[14] = {&s.x, &s.y, &s.z, &s.xd, &s.yd, &s.zd, &s.xdd, &s.ydd, &s.zdd,

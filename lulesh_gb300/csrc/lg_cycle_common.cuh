@@ -204,7 +204,7 @@ template <class M = IeeeOps>
 __device__ __forceinline__ void eval_eos(const Params &P, double e_in, double delv_in,
                                          double p_in, double q_in, double qq_in, double ql_in,
                                          double vnewc, int rep, double &p_out, double &e_out,
-                                         double &q_out, double &ss_out)
+                                         double &q_out, double &ss_out, bool need_ss = true)
 {
     const double rho0 = P.refdens;
     double p_new = 0., e_new = 0., q_new = 0., bvc = 0., pbvc = 0.;
@@ -267,7 +267,7 @@ __device__ __forceinline__ void eval_eos(const Params &P, double e_in, double de
     p_out = p_new;
     e_out = e_new;
     q_out = q_new;
-    ss_out = ssc_of<M>(pbvc * e_new + vnewc * vnewc * bvc * p_new, rho0);
+    ss_out = need_ss ? ssc_of<M>(pbvc * e_new + vnewc * vnewc * bvc * p_new, rho0) : 0.0;
 }
 
 __device__ __forceinline__ double dmin_sel(double a, double b) { return (b < a) ? b : a; }

@@ -72,6 +72,11 @@ struct DevState {
     double *e, *p, *q, *ql, *qq, *v, *volo, *vnew, *delv, *vdov, *arealg, *ss, *elemMass;
     double *delx_xi, *delx_eta, *delx_zeta, *delv_xi, *delv_eta, *delv_zeta;
     int *regNumList, *regPerm, *regRep;
+    // work items of k_material: regPerm / regRep hold nItems entries (one per
+    // element, or on small meshes several per element of the costly regions,
+    // each with a share of the EOS repetitions; the element's last one is its
+    // writer, regRep > 0; padding has regPerm < 0).  Ensembles: nItems = E.
+    int nItems;
     // per-corner force scratch, 6 * 8 * E doubles
     double *corner;
     // per-block minima of the time-constraint reduction

@@ -408,6 +408,7 @@ int lg_ensemble_create(int nprob, const lg_opts *opts, lg_ensemble **out)
     char *b = static_cast<char *>(en->arena);
     lg::DevState &s = en->ds;
     s.E = (int)E;
+    s.nItems = (int)E;
     s.N = (int)N;
     s.nx = 0;
     s.numReg = 0;

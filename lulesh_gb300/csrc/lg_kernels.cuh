@@ -349,14 +349,32 @@ __global__ void __launch_bounds__(BS) k_kinematics(DevState s)
     }
 }
 
-// One element at region-order position t: monotonic-Q limiter, qstop check,
-// material update (MODE != 1) and its Courant/hydro candidates (MODE != 0).
+// One work item of k_material: an element at region-order position t with
+// all its EOS repetitions, or on small meshes a share of them (see
+// upload_regions in lg_api.cu).  regRep[t] > 0 marks the element's writer,
+// which stores the update and the Courant/hydro candidates; < 0 marks a
+// share whose results are dropped; regPerm[t] < 0 is padding.  Every
+// repetition computes the same values from the same inputs, so the writer's
+// are the update.
+struct MatItem {
+    int ielem, reps;
+    bool writer;
+    double qlin, qquad, q_old, vnewc, vnew, e, delv, p;
+};
+
+// Phase 1, reads only: monotonic-Q limiter, qstop check and the material
+// clamps of item t (MODE != 1).  False for padding.
 template <int MODE>
-__device__ __forceinline__ void material_element(const DevState &s, const int t, Ctl *ctl,
-                                                 double &dtc, double &dth)
+__device__ __forceinline__ bool material_load(const DevState &s, const int t, Ctl *ctl,
+                                              MatItem &m)
 {
     const Params &P = s.prm;
     const int ielem = s.regPerm[t];
+    if (ielem < 0) return false;
+    const int r = s.regRep[t];
+    m.ielem = ielem;
+    m.writer = r > 0;
+    m.reps = r > 0 ? r : -r;
     if (MODE != 1) {
         // CalcMonotonicQRegionForElems, lulesh.cc:1761-1921
         const int bc = s.elemBC[ielem];
@@ -391,12 +409,12 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
                      delvxeta * delvxeta * (1. - phieta * phieta) +
                      delvxzeta * delvxzeta * (1. - phizeta * phizeta));
         }
-        s.qq[ielem] = qquad;
-        s.ql[ielem] = qlin;
+        m.qlin = qlin;
+        m.qquad = qquad;
 
         // qstop check on the previous cycle's q, lulesh.cc:1993-2008
-        const double q_old = s.q[ielem];
-        if (dlt(P.qstop, q_old)) ctl->err_qstop = 1;
+        m.q_old = s.q[ielem];
+        if (dlt(P.qstop, m.q_old)) ctl->err_qstop = 1;
 
         // ApplyMaterialPropertiesForElems, lulesh.cc:2328-2406
         double vnewc = vnew;
@@ -406,21 +424,42 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
         if (dnz(P.eosvmin) && dlt(vc, P.eosvmin)) vc = P.eosvmin;
         if (dnz(P.eosvmax) && dlt(P.eosvmax, vc)) vc = P.eosvmax;
         if (dle(vc, 0.)) ctl->err_matvol = 1;
-
-        double p_new, e_new, q_new, ss_new;
-        eval_eos(P, s.e[ielem], s.delv[ielem], s.p[ielem], q_old, qquad, qlin, vnewc,
-                 s.regRep[t], p_new, e_new, q_new, ss_new);
-        s.p[ielem] = p_new;
-        s.e[ielem] = e_new;
-        s.q[ielem] = q_new;
-        s.ss[ielem] = ss_new;
-
-        // UpdateVolumesForElems, lulesh.cc:2410-2427
-        double tmpV = vnew;
-        if (dabs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
-        s.v[ielem] = tmpV;
+        m.vnewc = vnewc;
+        m.vnew = vnew;
+        m.e = s.e[ielem];
+        m.delv = s.delv[ielem];
+        m.p = s.p[ielem];
     }
-    if (MODE != 0) {
+    return true;
+}
+
+// Phase 2: the item's EOS repetitions (MODE != 1); the writer stores the
+// update (MODE != 1) and its Courant/hydro candidates (MODE != 0).
+template <int MODE>
+__device__ __forceinline__ void material_update(const DevState &s, const MatItem &m,
+                                                double &dtc, double &dth)
+{
+    const Params &P = s.prm;
+    const int ielem = m.ielem;
+    if (MODE != 1) {
+        double p_new, e_new, q_new, ss_new;
+        eval_eos(P, m.e, m.delv, m.p, m.q_old, m.qquad, m.qlin, m.vnewc, m.reps, p_new, e_new,
+                 q_new, ss_new, m.writer);
+        if (m.writer) {
+            s.qq[ielem] = m.qquad;
+            s.ql[ielem] = m.qlin;
+            s.p[ielem] = p_new;
+            s.e[ielem] = e_new;
+            s.q[ielem] = q_new;
+            s.ss[ielem] = ss_new;
+
+            // UpdateVolumesForElems, lulesh.cc:2410-2427
+            double tmpV = m.vnew;
+            if (dabs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
+            s.v[ielem] = tmpV;
+        }
+    }
+    if (MODE != 0 && m.writer) {
         // CalcCourantConstraintForElems (2447-2513) and
         // CalcHydroConstraintForElems (2517-2572) for one element.  The
         // reference evaluates the Courant dt of every element but keeps it
@@ -455,7 +494,12 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
     double dtc = 1.0e+20, dth = 1.0e+20;
     if (!BATCHED) {
         const int t = blockIdx.x * BS + threadIdx.x;
-        if (t < s.E) material_element<MODE>(s, t, s.ctl, dtc, dth);
+        MatItem m;
+        const bool have = t < s.nItems && material_load<MODE>(s, t, s.ctl, m);
+        // An element's items share this block: every item has read the
+        // element's state before its writer stores the update.
+        __syncthreads();
+        if (have) material_update<MODE>(s, m, dtc, dth);
         if (MODE != 0)
             finish_dt<BS>(s, dtc, dth, MODE == 2);
         else
@@ -470,7 +514,9 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
         if (t < s.E) {
             pid = s.elemProb[s.regPerm[t]];
             Ctl *ctl = s.ctl + pid;
-            if (cycle_live(ctl)) material_element<2>(s, t, ctl, dtc, dth);
+            MatItem m;
+            if (cycle_live(ctl) && material_load<2>(s, t, ctl, m))
+                material_update<2>(s, m, dtc, dth);
         }
         batched_dt_candidates(s, pid, dtc, dth);
     }
