@@ -151,7 +151,7 @@ int upload_inv_mass(lg_domain *d, const double *m, size_t n)
 // On a small mesh the costly regions fill too few blocks to keep every SM's
 // FP64 pipe busy: at s=30 the 10(1+cost)-repetition elements make 35 blocks
 // for 152 SMs, which run their repetitions one after another while the other
-// SMs idle.  There (FP64 builds) the elements of each repetition count whose
+// SMs idle.  There the elements of each repetition count whose
 // elements number fewer than T (three blocks of 128 per SM) get f items that
 // share their repetitions, f = min(ceil(T / count), rep, 32).  All items of
 // an element sit in one block of 128 (padding where a group would straddle
@@ -167,10 +167,9 @@ int upload_regions(lg_domain *d)
     for (int r = 0; r < p.numReg; ++r)
         count[lg::region_rep(r, p.numReg, p.cost)] += (long long)p.regElemlist[r].size();
     const long long T = 3LL * d->resident / 8;
-    const bool split = d->opts.precision != LG_MIXED;
     auto items_of = [&](int rr) -> int {
         const long long n = count[rr];
-        if (!split || rr < 2 || n >= T || n == 0) return 1;
+        if (rr < 2 || n >= T || n == 0) return 1;
         return (int)std::min<long long>({(T + n - 1) / n, (long long)rr, 32LL});
     };
     std::vector<int> perm, rep;

@@ -497,8 +497,9 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
         MatItem m;
         const bool have = t < s.nItems && material_load<MODE>(s, t, s.ctl, m);
         // An element's items share this block: every item has read the
-        // element's state before its writer stores the update.
-        __syncthreads();
+        // element's state before its writer stores the update.  Without
+        // shared elements (nItems == E) no item waits for another.
+        if (s.nItems != s.E) __syncthreads();
         if (have) material_update<MODE>(s, m, dtc, dth);
         if (MODE != 0)
             finish_dt<BS>(s, dtc, dth, MODE == 2);

@@ -321,7 +321,10 @@ __global__ void __launch_bounds__(BS) k_kinematics(DevState s)
 }
 
 // Q limiter (FP32) + material update (FP64 EOS) + time constraints (FP64)
-// for one element at region-order position t; MODE as in the FP64 kernels
+// for one element at region-order position t holding all its repetitions
+// (nItems == E, and the batched kernel); MODE as in the FP64 kernels.  Kept
+// beside the two-phase form: it measures 1.5 % faster when no element is
+// shared.
 template <int MODE>
 __device__ __forceinline__ void material_element(const DevState &s, const int t, Ctl *ctl,
                                                  double &dtc, double &dth)
@@ -410,6 +413,131 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
     }
 }
 
+// One work item of k_material, as in the FP64 kernels (MatItem there):
+// regRep > 0 the element's writer, < 0 a share of its EOS repetitions,
+// regPerm < 0 padding.
+struct MatItem {
+    int ielem, reps;
+    bool writer;
+    double qlin, qquad, q_old, vnewc, vnew, e, delv, p;
+};
+
+// Phase 1, reads only: Q limiter (FP32), qstop check and material clamps
+// (MODE != 1).  False for padding.
+template <int MODE>
+__device__ __forceinline__ bool material_load(const DevState &s, const int t, Ctl *ctl,
+                                              MatItem &m)
+{
+    const Params &P = s.prm;
+    const int ielem = s.regPerm[t];
+    if (ielem < 0) return false;
+    const int r = s.regRep[t];
+    m.ielem = ielem;
+    m.writer = r > 0;
+    m.reps = r > 0 ? r : -r;
+    if (MODE != 1) {
+        const float lm = to_f32(P.monoq_limiter_mult), ms = to_f32(P.monoq_max_slope);
+        const float *gvx = fview(s.delv_xi), *gve = fview(s.delv_eta),
+                    *gvz = fview(s.delv_zeta);
+        const int bc = s.elemBC[ielem];
+        const float phixi = monoq_phi(lm, ms, gvx, ielem, bc, XI_M_SYMM, XI_M_FREE, XI_M,
+                                      XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
+                                      s.lxip[ielem]);
+        const float phieta = monoq_phi(lm, ms, gve, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
+                                       ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P, s.letam[ielem],
+                                       s.letap[ielem]);
+        const float phizeta = monoq_phi(lm, ms, gvz, ielem, bc, ZETA_M_SYMM, ZETA_M_FREE,
+                                        ZETA_M, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P,
+                                        s.lzetam[ielem], s.lzetap[ielem]);
+        const double vnew = s.vnew[ielem];
+        const double vdov = s.vdov[ielem];
+        double qlin, qquad;
+        if (FastOps::lt(0.0, vdov)) {
+            qlin = 0.;
+            qquad = 0.;
+        } else {
+            float dxxi = gvx[ielem] * fview(s.delx_xi)[ielem];
+            float dxeta = gve[ielem] * fview(s.delx_eta)[ielem];
+            float dxzeta = gvz[ielem] * fview(s.delx_zeta)[ielem];
+            if (dxxi > 0.f) dxxi = 0.f;
+            if (dxeta > 0.f) dxeta = 0.f;
+            if (dxzeta > 0.f) dxzeta = 0.f;
+            const float rho = to_f32(s.elemMass[ielem]) /
+                              (to_f32(s.volo[ielem]) * to_f32(vnew));
+            qlin = to_f64(-to_f32(P.qlc_monoq) * rho *
+                          (dxxi * (1.f - phixi) + dxeta * (1.f - phieta) +
+                           dxzeta * (1.f - phizeta)));
+            qquad = to_f64(to_f32(P.qqc_monoq) * rho *
+                           (dxxi * dxxi * (1.f - phixi * phixi) +
+                            dxeta * dxeta * (1.f - phieta * phieta) +
+                            dxzeta * dxzeta * (1.f - phizeta * phizeta)));
+        }
+        m.qlin = qlin;
+        m.qquad = qquad;
+
+        m.q_old = s.q[ielem];
+        if (FastOps::lt(P.qstop, m.q_old)) ctl->err_qstop = 1;
+
+        double vnewc = vnew;
+        if (P.eosvmin != 0. && FastOps::lt(vnewc, P.eosvmin)) vnewc = P.eosvmin;
+        if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vnewc)) vnewc = P.eosvmax;
+        double vc = s.v[ielem];
+        if (P.eosvmin != 0. && FastOps::lt(vc, P.eosvmin)) vc = P.eosvmin;
+        if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vc)) vc = P.eosvmax;
+        if (FastOps::le(vc, 0.)) ctl->err_matvol = 1;
+        m.vnewc = vnewc;
+        m.vnew = vnew;
+        m.e = s.e[ielem];
+        m.delv = s.delv[ielem];
+        m.p = s.p[ielem];
+    }
+    return true;
+}
+
+// Phase 2: the item's FP64 EOS repetitions (MODE != 1); the writer stores
+// the update (MODE != 1) and its FP64 Courant/hydro candidates (MODE != 0).
+template <int MODE>
+__device__ __forceinline__ void material_update(const DevState &s, const MatItem &m,
+                                                double &dtc, double &dth)
+{
+    const Params &P = s.prm;
+    const int ielem = m.ielem;
+    if (MODE != 1) {
+        double p_new, e_new, q_new, ss_new;
+        eval_eos<FastOps>(P, m.e, m.delv, m.p, m.q_old, m.qquad, m.qlin, m.vnewc, m.reps,
+                          p_new, e_new, q_new, ss_new, m.writer);
+        if (m.writer) {
+            s.qq[ielem] = m.qquad;
+            s.ql[ielem] = m.qlin;
+            s.p[ielem] = p_new;
+            s.e[ielem] = e_new;
+            s.q[ielem] = q_new;
+            s.ss[ielem] = ss_new;
+
+            double tmpV = m.vnew;
+            if (FastOps::abs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
+            s.v[ielem] = tmpV;
+        }
+    }
+    if (MODE != 0 && m.writer) {
+        // Only elements with vdov != 0 constrain dt; a warp of elements at
+        // rest skips the FP64 square root and reciprocals altogether.
+        const double vdov = s.vdov[ielem];
+        const bool moving = ((unsigned long long)__double_as_longlong(vdov) << 1) != 0ull;
+        if (__any_sync(__activemask(), moving) && moving) {
+            const double qqc2 = 64.0 * P.qqc * P.qqc;
+            const double ssv = s.ss[ielem];
+            const double arealg = s.arealg[ielem];
+            double dtf = ssv * ssv;
+            if (FastOps::lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
+            dtf = arealg * rcp_nr(sqrt_nr(dtf));
+            if (dtf < dtc) dtc = dtf;
+            const double dtdvov = P.dvovmax * rcp_nr(fabs(vdov) + 1.e-20);
+            if (dth > dtdvov) dth = dtdvov;
+        }
+    }
+}
+
 template <int MODE, bool BATCHED, int BS>
 __global__ void __launch_bounds__(BS) k_material(DevState s)
 {
@@ -417,7 +545,16 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
     double dtc = 1.0e+20, dth = 1.0e+20;
     if (!BATCHED) {
         const int t = blockIdx.x * BS + threadIdx.x;
-        if (t < s.E) material_element<MODE>(s, t, s.ctl, dtc, dth);
+        if (s.nItems == s.E) {
+            if (t < s.E) material_element<MODE>(s, t, s.ctl, dtc, dth);
+        } else {
+            MatItem m;
+            const bool have = t < s.nItems && material_load<MODE>(s, t, s.ctl, m);
+            // An element's items share this block: every item has read the
+            // element's state before its writer stores the update.
+            __syncthreads();
+            if (have) material_update<MODE>(s, m, dtc, dth);
+        }
         if (MODE != 0)
             finish_dt<BS>(s, dtc, dth, MODE == 2);
         else
