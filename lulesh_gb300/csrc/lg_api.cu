@@ -8,7 +8,6 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
-#include <map>
 #include <vector>
 
 #include "lg_device.h"
@@ -143,57 +142,21 @@ int upload_inv_mass(lg_domain *d, const double *m, size_t n)
     return upload(d, d->ds.invMass, inv);
 }
 
-// regNumList and k_material's work items (DevState::nItems) from the host
-// region sets: elements in region order, the regions with the most EOS
-// repetitions first (lg::region_visit_order), each region's elements in their
-// ascending regElemlist order, each item with its repetition count.
-//
-// On a small mesh the costly regions fill too few blocks to keep every SM's
-// FP64 pipe busy: at s=30 the 10(1+cost)-repetition elements make 35 blocks
-// for 152 SMs, which run their repetitions one after another while the other
-// SMs idle.  There the elements of each repetition count whose
-// elements number fewer than T (three blocks of 128 per SM) get f items that
-// share their repetitions, f = min(ceil(T / count), rep, 32).  All items of
-// an element sit in one block of 128 (padding where a group would straddle
-// two), so the kernel's barrier orders every item's reads before the
-// writer's stores.  The work done and the results are unchanged.
+// regNumList and k_material's work items (DevState::nItems), built on the
+// host by lg::build_work_items: elements in region order, the regions with
+// the most EOS repetitions first, each region's elements in their ascending
+// regElemlist order.  On a small mesh the costly regions fill too few blocks
+// to keep every SM's FP64 pipe busy (at s=30 the 8,445 elements with 20
+// repetitions make 66 blocks for 152 SMs), so their elements get several
+// items that share the repetitions.  All items of an element sit in one
+// block of 128, and the kernel's barrier orders every item's reads before
+// the writer's stores: the work done and the results are unchanged.
 int upload_regions(lg_domain *d)
 {
     const lg::Problem &p = d->prob;
-    const int E = p.numElem;
-    const std::vector<int> order = lg::region_visit_order(p.numReg, p.cost);
-    // elements per repetition count
-    std::map<int, long long> count;
-    for (int r = 0; r < p.numReg; ++r)
-        count[lg::region_rep(r, p.numReg, p.cost)] += (long long)p.regElemlist[r].size();
-    const long long T = 3LL * d->resident / 8;
-    auto items_of = [&](int rr) -> int {
-        const long long n = count[rr];
-        if (rr < 2 || n >= T || n == 0) return 1;
-        return (int)std::min<long long>({(T + n - 1) / n, (long long)rr, 32LL});
-    };
     std::vector<int> perm, rep;
-    perm.reserve(E);
-    rep.reserve(E);
-    int writers = 0;
-    for (const int r : order) {
-        const int rr = lg::region_rep(r, p.numReg, p.cost);
-        const int f = items_of(rr);
-        for (int e : p.regElemlist[r]) {
-            if (f > 1 && (int)(perm.size() % 128) + f > 128)
-                while (perm.size() % 128) {
-                    perm.push_back(-1);
-                    rep.push_back(0);
-                }
-            for (int i = 0; i < f; ++i) {
-                const int share = rr / f + (i < rr % f ? 1 : 0);
-                perm.push_back(e);
-                rep.push_back(i == f - 1 ? share : -share);
-            }
-            ++writers;
-        }
-    }
-    if (writers != E) return set_error(LG_ERR_INVALID, "region sets do not cover all elements");
+    if (lg::build_work_items(p, d->resident, 128, perm, rep) != p.numElem)
+        return set_error(LG_ERR_INVALID, "region sets do not cover all elements");
     if ((long long)perm.size() > d->item_cap)
         return set_error(LG_ERR_STATE, "%zu work items exceed the capacity %d", perm.size(),
                          d->item_cap);

@@ -2,6 +2,7 @@
 #include "lg_problem.h"
 
 #include <algorithm>
+#include <map>
 
 #include <cmath>
 #include <cstdio>
@@ -86,6 +87,44 @@ std::vector<int> region_visit_order(int numReg, int cost)
         return region_rep(a, numReg, cost) > region_rep(b, numReg, cost);
     });
     return order;
+}
+
+int build_work_items(const Problem &p, long long resident, int block,
+                     std::vector<int> &item_elem, std::vector<int> &item_rep)
+{
+    // elements per repetition count
+    std::map<int, long long> count;
+    for (int r = 0; r < p.numReg; ++r)
+        count[region_rep(r, p.numReg, p.cost)] += (long long)p.regElemlist[r].size();
+    const long long T = 3 * resident / 8;
+    auto items_of = [&](int rr) -> int {
+        const long long n = count[rr];
+        if (rr < 2 || n >= T || n == 0) return 1;
+        return (int)std::min<long long>({(T + n - 1) / n, (long long)rr, 32LL});
+    };
+    item_elem.clear();
+    item_rep.clear();
+    item_elem.reserve(p.numElem);
+    item_rep.reserve(p.numElem);
+    int writers = 0;
+    for (const int r : region_visit_order(p.numReg, p.cost)) {
+        const int rr = region_rep(r, p.numReg, p.cost);
+        const int f = items_of(rr);
+        for (int e : p.regElemlist[r]) {
+            if (f > 1 && (int)(item_elem.size() % block) + f > block)
+                while (item_elem.size() % block) {
+                    item_elem.push_back(-1);
+                    item_rep.push_back(0);
+                }
+            for (int i = 0; i < f; ++i) {
+                const int share = rr / f + (i < rr % f ? 1 : 0);
+                item_elem.push_back(e);
+                item_rep.push_back(i == f - 1 ? share : -share);
+            }
+            ++writers;
+        }
+    }
+    return writers;
 }
 
 void build_corner_list(Problem &p)

@@ -98,6 +98,19 @@ int region_rep(int r, int numReg, int cost);
 // the grid keeps them from forming a tail that leaves SMs idle.
 std::vector<int> region_visit_order(int numReg, int cost);
 
+// Work items of the material kernel (one per element, or on a small mesh
+// several per element of a costly repetition count, each with a share of the
+// element's EOS repetitions).  Fills item_elem (element id, -1 for padding)
+// and item_rep (> 0: the element's writer with that many repetitions, < 0: a
+// share of -item_rep repetitions, 0: padding), in region visit order.  A
+// repetition count whose elements number fewer than 3/8 of `resident` (the
+// threads of one resident wave) gets f = min(ceil(T / count), rep, 32) items
+// per element, T = 3/8 resident; an element's items never straddle a block
+// of `block` threads.  Returns the number of writers, which is numElem when
+// the region sets cover every element once.
+int build_work_items(const Problem &p, long long resident, int block,
+                     std::vector<int> &item_elem, std::vector<int> &item_rep);
+
 // End-of-run report text, lulesh-util.cc:175-230.
 std::string format_report(int nx, int cycle, double e0, double maxAbsDiff,
                           double totalAbsDiff, double maxRelDiff, double elapsed);

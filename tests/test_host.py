@@ -3,6 +3,7 @@ exports the declared C ABI, the problem set-up matches the oracle's, and the
 command line parses the reference options."""
 import os
 import re
+import shutil
 import subprocess
 
 import numpy as np
@@ -127,3 +128,20 @@ def test_ensemble_sample_is_deterministic_and_in_range(native_lib):
         assert 1.0 <= m["hgcoef"] <= 3.0 and 0.5 <= m["einit_factor"] <= 2.0
         assert m["balance"] == 1 and m["cost"] == 1 and m["its"] == 300
     assert len({m["nx"] for m in a}) > 20  # the sizes really vary
+
+
+def test_material_work_items(tmp_path):
+    """lg::build_work_items on the reference's region draws: one writer per
+    element, shares adding up to the region's repetitions, an element's items
+    within one block, within the reserved capacity (work_items_selftest.cc)."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    csrc = os.path.join(root, "lulesh_gb300", "csrc")
+    exe = tmp_path / "work_items_selftest"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", csrc,
+                    os.path.join(root, "tests", "work_items_selftest.cc"),
+                    os.path.join(csrc, "lg_problem.cc"), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert r.stdout.strip().endswith("failed checks 0"), r.stdout[-3000:]
