@@ -12,11 +12,13 @@
 //   k_kinematics  per element: volume, vnew, delv, arealg, vdov
 //                 (CalcKinematicsForElems) and the monotonic-Q gradients
 //                 (CalcMonotonicQGradientsForElems)
-//   k_material    per element in region order: monotonic-Q limiter, qstop
-//                 check, EOS with its repetitions, sound speed, volume
-//                 update, Courant/hydro constraints with a block reduction;
-//                 its last block finishes the reduction and runs the next
-//                 cycle's TimeIncrement
+//   k_material    per work item in region order (an element, or on small
+//                 meshes a share of an element's EOS repetitions):
+//                 monotonic-Q limiter, qstop check, EOS with its
+//                 repetitions, sound speed, volume update, Courant/hydro
+//                 constraints with a block reduction; its last block
+//                 finishes the reduction and runs the next cycle's
+//                 TimeIncrement
 //
 // Every arithmetic expression keeps the reference's operand order (see the
 // oracle's lulesh_oracle.c for the line-by-line correspondence), with two
