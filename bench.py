@@ -18,6 +18,11 @@ Prints one JSON line.  `value` is the device-timed rate (CUDA events on the
 handle's stream around exactly K cycles, the state resident in HBM);
 `e2e` is the same metric through the C ABI with host buffers: upload of every
 Domain field from pinned host memory, the K cycles, download of every field.
+`subrecords` measures, in the same run, every other configuration the metric
+names (config 1 at s=30; config 2's full 500 cycles in both FP64 builds; the
+mixed build at s=192, 16 regions, balance 2, cost 4 with its errors against
+the strict FP64 run; the 64-member ensemble batched and member by member);
+`--no-subrecords` skips them.
 `--impl reference` times the reference algorithm on the host cores instead
 (the oracle's C restatement, -O3 OpenMP, all host threads), on the same
 workload.  Under torchrun each rank runs an independent replica of the
@@ -392,6 +397,113 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def _timed_single(lg, nx, nr, b, c, cycles, precision, device, warmup=3):
+    """A fresh problem: warm-up cycles, reset, then `cycles` device-timed
+    cycles from the initial state.  Returns (handle, record)."""
+    d = lg.Domain(nx, nr, b, c, its=10 ** 9, precision=precision, device=device)
+    if warmup:
+        d.step(warmup)
+    d.reset()
+    st, ms = d.step_timed(cycles)
+    if st != 0:
+        raise SystemExit(f"s={nx} {precision}: run failed with status {st}")
+    return d, {"value": nx ** 3 * cycles / (ms * 1e3), "unit": UNIT, "cycles": cycles,
+               "ms_per_cycle": ms / cycles, "precision": precision,
+               "origin_energy": d.field("e")[0]}
+
+
+def _errors(d, ref) -> dict:
+    """Errors of handle d against handle ref after the same cycles: origin
+    energy, total energy (internal + kinetic), the energy field normwise, and
+    both runs' plane-0 symmetry deltas (lulesh-util.cc:197-212)."""
+    import numpy as np
+    vm, vf = d.verify(), ref.verify()
+    em, ef = d.field("e"), ref.field("e")
+    return {"origin_energy_rel": abs(vm["origin_energy"] / vf["origin_energy"] - 1),
+            "total_energy_rel": abs(_total_energy(d) / _total_energy(ref) - 1),
+            "e_normwise": float(np.max(np.abs(em - ef)) / np.max(np.abs(ef))),
+            "symmetry_MaxRelDiff": vm["MaxRelDiff"], "symmetry_MaxRelDiff_ref": vf["MaxRelDiff"],
+            "symmetry_MaxAbsDiff": vm["MaxAbsDiff"], "symmetry_MaxAbsDiff_ref": vf["MaxAbsDiff"]}
+
+
+def _ensemble_rates(lg, members, precision, cycles, device, warmup=2) -> dict:
+    """Batched rate of the members (autotuned, device-timed) and the plain
+    path's rate running them one by one, same cycles."""
+    en = lg.Ensemble(members, precision=precision, device=device)
+    E = en.info()["elements"]
+    tune = en.autotune(3)
+    if warmup:
+        en.step(warmup)
+    en.reset()
+    st, ms = en.step_timed(cycles)
+    if st != 0:
+        raise SystemExit(f"ensemble {precision}: status {st}")
+    en.close()
+    seq_ms = 0.0
+    for m in members:
+        d = lg.Domain(m["nx"], m["numReg"], m["balance"], m["cost"], its=10 ** 9,
+                      hgcoef=m["hgcoef"], einit_factor=m["einit_factor"],
+                      precision=precision, device=device)
+        d.step(warmup)
+        d.reset()
+        _, t = d.step_timed(cycles)
+        seq_ms += t
+        d.close()
+    batched, seq = E * cycles / (ms * 1e3), E * cycles / (seq_ms * 1e3)
+    return {"value": batched, "unit": UNIT, "sequential_plain": seq,
+            "batched_over_sequential": batched / seq, "elements": E, "cycles": cycles,
+            "precision": precision, "autotune": {k: v["block"] * (-1 if v["persistent"] else 1)
+                                                  for k, v in tune.items()}}
+
+
+def subrecords(a, device: int) -> dict:
+    """Every configuration the metric names, measured in the same run as the
+    headline (device-timed, each from its initial state after warm-up):
+      config1:      s=30, 11 regions, 100 cycles, each arithmetic
+      config2_full: s=150, 11 regions, 500 cycles, both FP64 builds
+      mixed:        s=192, 16 regions, balance 2, cost 4, 500 cycles: mixed and
+                    strict FP64 (the error reference), FP64+FMA over 100 cycles
+      ensemble:     the 64-member study set (seed 0), 300 cycles, batched and
+                    member by member, FP64+FMA and mixed"""
+    import lulesh_gb300 as lg
+    out = {}
+    c1 = {}
+    for prec in ("fp64", "fp64-fma", "mixed"):
+        d, r = _timed_single(lg, 30, 11, 1, 1, 100, prec, device)
+        c1[prec] = r
+        d.close()
+    out["config1"] = {"workload": "Sedov s=30 (27,000 elements), 11 regions, b1 c1, 100 cycles",
+                      **c1}
+    c2 = {}
+    for prec in ("fp64-fma", "fp64"):
+        d, r = _timed_single(lg, 150, 11, 1, 1, 500, prec, device)
+        c2[prec] = r
+        d.close()
+    out["config2_full"] = {"workload": "Sedov s=150 (3,375,000 elements), 11 regions, b1 c1, "
+                                       "500 cycles", **c2}
+    dm, rm = _timed_single(lg, 192, 16, 2, 4, 500, "mixed", device)
+    df, rf = _timed_single(lg, 192, 16, 2, 4, 500, "fp64", device)
+    err = _errors(dm, df)
+    dm.close()
+    df.close()
+    dfa, rfa = _timed_single(lg, 192, 16, 2, 4, 100, "fp64-fma", device)
+    dfa.close()
+    out["mixed"] = {"workload": "Sedov s=192 (7,077,888 elements), 16 regions, balance 2, cost "
+                                "4, 500 cycles", "mixed": rm, "fp64": rf, "fp64-fma_100_cycles": rfa,
+                    "mixed_over_fp64": rm["value"] / rf["value"],
+                    "mixed_over_fp64_fma": rm["value"] / rfa["value"],
+                    "err_vs_fp64": err,
+                    "err_reference": "the strict FP64 GPU run of the same 500 cycles"}
+    members = lg.sample_ensemble(64, seed=0)
+    for m in members:
+        m["its"] = 10 ** 9
+    out["ensemble"] = {"workload": "64 sampled Sedov problems (seed 0: s 16..64, energy x "
+                                   "[0.5, 2], hgcoef [1, 3], 4..16 regions), 300 cycles",
+                       "fp64-fma": _ensemble_rates(lg, members, "fp64-fma", 300, device),
+                       "mixed": _ensemble_rates(lg, members, "mixed", 300, device)}
+    return out
+
+
 def run_gpu(a):
     dist, ws, rank, local = _dist()
     import numpy as np
@@ -510,6 +622,13 @@ def run_gpu(a):
             "origin_energy": verify["origin_energy"]}
     if a.err_vs_fp64 and a.precision != "fp64":
         line["err_vs_fp64"] = error_vs_fp64(a, d)
+    d.close()
+    if ws == 1 and not a.no_subrecords:
+        with ClockSampler(local) as clk_sub:
+            t_sub = time.perf_counter()
+            line["subrecords"] = subrecords(a, local)
+            line["subrecords"]["wall_s"] = time.perf_counter() - t_sub
+        line["subrecords"]["clocks"] = clk_sub.summary()
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference_rate(
             a, budget_s=float(os.environ.get("LG_CPU_BUDGET_S", "15")), warmup=1,
@@ -535,6 +654,9 @@ def main():
                         "reference's arithmetic operation for operation); mixed: FP32 "
                         "forces/kinematics/Q with FP64 state and EOS")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-subrecords", action="store_true",
+                   help="skip the other configurations' records (config 1, config 2 over 500 "
+                        "cycles, mixed s=192, the 64-member ensemble; about 80 s)")
     p.add_argument("--ensemble", type=int, default=0,
                    help="batched ensemble of this many sampled problems instead of one problem")
     p.add_argument("--seed", type=int, default=0, help="ensemble sample seed")

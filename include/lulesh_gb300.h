@@ -231,6 +231,78 @@ int lg_ensemble_get_scalar(lg_ensemble *en, int prob, const char *name, double *
  * may be NULL). */
 int lg_ensemble_autotune(lg_ensemble *en, int ncycles, int *block_sizes, int *persistent);
 
+/* ---------------------------------------------------------------------------
+ * Halo exchange of a block decomposition.  The reference runs one Domain per
+ * MPI rank on a tp x tp x tp grid of cubes of nx elements (InitMeshDecomp,
+ * lulesh-init.cc:676-738; rank = col + row*tp + plane*tp^2) and exchanges
+ * boundary values with up to 26 neighbours (6 faces, 12 edges, 8 corners):
+ *   LG_HALO_SBN           CommSend + CommSBN (lulesh-comm.cc:357, 848): node
+ *                         fields; each neighbour's values at the shared nodes
+ *                         are added, message after message (forces,
+ *                         lulesh.cc:1109-1133; nodal mass, lulesh.cc:2723-2729)
+ *   LG_HALO_SYNC_POS_VEL  CommSend + CommSyncPosVel (357, 1261): node fields;
+ *                         shared nodes take the higher-ranked neighbour's
+ *                         values (lulesh.cc:2621-2642)
+ *   LG_HALO_MONOQ         CommSend + CommMonoQ (357, 1684): element fields of
+ *                         the six face neighbours' boundary layers, copied into
+ *                         ghost elements after numElem (lulesh.cc:1963-1985)
+ * A plan lists one rank's messages in the reference's order and buffer layout
+ * (CommRecv/CommSend, lulesh-comm.cc:59-845: faces, edges, corners at
+ * pmsg*maxPlaneComm + emsg*maxEdgeComm + cmsg*16 doubles, the fields of a
+ * message one after another), so send and receive buffers are
+ * interchangeable with the reference's commDataSend / commDataRecv.  Packing
+ * and unpacking run on the GPU; moving each message to its peer's receive
+ * buffer (MPI, NCCL, peer copies) is the caller's, as MPI_Isend / MPI_Irecv
+ * are the reference's.
+ * ------------------------------------------------------------------------- */
+enum lg_halo_kind { LG_HALO_SBN = 0, LG_HALO_SYNC_POS_VEL = 1, LG_HALO_MONOQ = 2 };
+
+typedef struct lg_halo_plan lg_halo_plan;
+
+typedef struct lg_halo_info {
+    size_t buffer_doubles; /* send and receive buffer length: the reference's
+                              comBufSize (lulesh-init.cc:358-380) */
+    int send_messages, recv_messages;
+    int send_values, recv_values; /* values per field, summed over the messages */
+    int recv_targets;   /* distinct lattice points (or ghost slots) written */
+    int ghost_elems;    /* LG_HALO_MONOQ: ghost elements after numElem */
+    int field_length;   /* entries each field array must hold: nodes (nx+1)^3,
+                           or numElem + ghost_elems */
+} lg_halo_info;
+
+/* The plan of rank `rank` of a tp^3 decomposition of cubes of nx elements
+ * for nfields fields (1..6; the reference sends 3 forces, 1 nodal mass, 6
+ * positions and velocities, 3 velocity gradients).  Host-only: the plan's
+ * device copy is made on the current device by its first pack or unpack. */
+int lg_halo_plan_create(int kind, int nx, int tp, int rank, int nfields, lg_halo_plan **out);
+void lg_halo_plan_destroy(lg_halo_plan *plan);
+int lg_halo_plan_info(const lg_halo_plan *plan, lg_halo_info *info);
+
+/* Message m (in order) of direction dir (0 send, 1 receive): the peer rank,
+ * the values per field, and the message's offset in the buffer (doubles);
+ * the message occupies nfields * count doubles from there. */
+int lg_halo_plan_message(const lg_halo_plan *plan, int dir, int m, int *peer, int *count,
+                         size_t *offset);
+
+/* The plan's value list (n = send_values or recv_values): for dir 0, the
+ * lattice index packed at buffer position bufpos[k] (field f at bufpos[k] +
+ * f*stride[k]); for dir 1, the lattice index (or ghost slot) each received
+ * value goes to, grouped by target in the order the values are applied.
+ * Any output may be NULL. */
+int lg_halo_plan_entries(const lg_halo_plan *plan, int dir, int *index, int *bufpos, int *stride,
+                         size_t n);
+
+/* Pack fields[0..nfields) (device arrays of field_length doubles; fields is
+ * a host array of device pointers) into send_buf (device, buffer_doubles),
+ * on stream (a cudaStream_t or NULL).  Asynchronous. */
+int lg_halo_pack(lg_halo_plan *plan, double *const *fields, double *send_buf, void *stream);
+
+/* Apply the received messages in recv_buf (device, buffer_doubles) to the
+ * fields in the reference's message order: added for LG_HALO_SBN, copied
+ * otherwise.  Deterministic (no atomics).  Asynchronous on stream. */
+int lg_halo_unpack(lg_halo_plan *plan, double *const *fields, const double *recv_buf,
+                   void *stream);
+
 /* Nodal forces with no device allocation, for callers that own all device
  * memory themselves.  No counterpart in the reference: it exists for codes
  * that cannot let a library allocate behind their back -- hydro codes that
@@ -253,9 +325,12 @@ int lg_ensemble_autotune(lg_ensemble *en, int ncycles, int *block_sizes, int *pe
  * most 32768 elements (about 12.6 MB, held on every GPU where the call has
  * run until the process exits); larger meshes are rejected with
  * LG_ERR_INVALID.  The first call on each device looks up that array's
- * device address, so make it before any stream capture on that device.  All
- * calls share the array: calls whose work overlaps on one GPU race and must
- * be serialised by the caller. */
+ * device address; make that first call before any stream capture on the
+ * device.  Every call reads its status word back and so blocks the host
+ * until its kernels have finished.  A non-sticky CUDA error left pending by
+ * the caller's earlier work is cleared on entry, so that a failure reported
+ * here is this call's own.  All calls share the array: calls whose work
+ * overlaps on one GPU race and must be serialised by the caller. */
 int lg_calc_force_for_nodes_noalloc(int numElem, int numNode, const int *nodelist,
                                     const int *nodeElemStart, const int *nodeElemCornerList,
                                     const double *x, const double *y, const double *z,

@@ -23,7 +23,8 @@ import os
 import numpy as np
 
 __all__ = ["Domain", "LuleshError", "VolumeError", "QStopError", "library_path", "load",
-           "FP64", "FP64_FMA", "MIXED", "NODE_FIELDS", "ELEM_FIELDS", "measure_pipe", "Ensemble", "sample_ensemble"]
+           "FP64", "FP64_FMA", "MIXED", "NODE_FIELDS", "ELEM_FIELDS", "measure_pipe", "Ensemble",
+           "sample_ensemble", "HaloPlan", "HALO_KINDS"]
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_PKG, "lib", "liblulesh_gb300.so")
@@ -58,6 +59,13 @@ class _Opts(ctypes.Structure):
                 ("cost", ctypes.c_int), ("its", ctypes.c_int), ("precision", ctypes.c_int),
                 ("hgcoef", ctypes.c_double), ("einit_factor", ctypes.c_double),
                 ("device", ctypes.c_int)]
+
+
+class _HaloInfo(ctypes.Structure):
+    _fields_ = [("buffer_doubles", ctypes.c_size_t), ("send_messages", ctypes.c_int),
+                ("recv_messages", ctypes.c_int), ("send_values", ctypes.c_int),
+                ("recv_values", ctypes.c_int), ("recv_targets", ctypes.c_int),
+                ("ghost_elems", ctypes.c_int), ("field_length", ctypes.c_int)]
 
 
 _lib = None
@@ -122,6 +130,16 @@ def load() -> ctypes.CDLL:
     lib.lg_ensemble_autotune.argtypes = [H, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                          ctypes.POINTER(ctypes.c_int)]
     lib.lg_measure_pipe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.lg_halo_plan_create.argtypes = [ctypes.c_int] * 5 + [ctypes.POINTER(H)]
+    lib.lg_halo_plan_destroy.argtypes = [H]
+    lib.lg_halo_plan_info.argtypes = [H, ctypes.POINTER(_HaloInfo)]
+    lib.lg_halo_plan_message.argtypes = [H, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_size_t)]
+    lib.lg_halo_plan_entries.argtypes = [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_size_t]
+    lib.lg_halo_pack.argtypes = [H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.lg_halo_unpack.argtypes = [H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.lg_last_error.restype = ctypes.c_char_p
     _lib = lib
     return lib
@@ -487,5 +505,91 @@ class Ensemble:
         """Replace a member's double field (lg_ensemble_set_field)."""
         a = np.ascontiguousarray(values, dtype=np.float64)
         st = self._lib.lg_ensemble_set_field(self._h, member, name.encode(), a.ctypes.data, a.size)
+        if st:
+            _raise(st, self._lib)
+
+
+HALO_KINDS = {"sbn": 0, "sync_pos_vel": 1, "monoq": 2}
+
+
+def _dev_ptr(a) -> int:
+    """Device address of a torch tensor, or an integer address as is."""
+    return a.data_ptr() if hasattr(a, "data_ptr") else int(a)
+
+
+class HaloPlan:
+    """One rank's halo messages of a tp^3 block decomposition (lg_halo_*):
+    kind "sbn" (CommSBN: node fields summed), "sync_pos_vel" (CommSyncPosVel:
+    node fields copied from higher ranks) or "monoq" (CommMonoQ: element
+    fields into ghost elements), in the reference's message order and buffer
+    layout (lulesh-comm.cc).  pack / unpack take device arrays (torch
+    tensors or addresses) and run on the GPU; the plan itself is host data."""
+
+    def __init__(self, kind, nx: int, tp: int, rank: int, nfields: int):
+        lib = load()
+        self._lib = lib
+        h = ctypes.c_void_p()
+        k = HALO_KINDS[kind] if isinstance(kind, str) else int(kind)
+        st = lib.lg_halo_plan_create(k, nx, tp, rank, nfields, ctypes.byref(h))
+        if st:
+            _raise(st, lib)
+        self._h = h
+        self.kind, self.nx, self.tp, self.rank, self.nfields = k, nx, tp, rank, nfields
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lg_halo_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        i = _HaloInfo()
+        st = self._lib.lg_halo_plan_info(self._h, ctypes.byref(i))
+        if st:
+            _raise(st, self._lib)
+        return {k: getattr(i, k) for k, _ in _HaloInfo._fields_}
+
+    def messages(self, side: str) -> list[dict]:
+        """side "send" or "recv": [{peer, count, offset}] in order."""
+        d = 0 if side == "send" else 1
+        n = self.info()["send_messages" if d == 0 else "recv_messages"]
+        out = []
+        for m in range(n):
+            peer, count, off = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+            st = self._lib.lg_halo_plan_message(self._h, d, m, ctypes.byref(peer),
+                                                ctypes.byref(count), ctypes.byref(off))
+            if st:
+                _raise(st, self._lib)
+            out.append({"peer": peer.value, "count": count.value, "offset": off.value})
+        return out
+
+    def entries(self, side: str) -> dict:
+        """The plan's value list: index, bufpos, stride (numpy int32)."""
+        d = 0 if side == "send" else 1
+        n = self.info()["send_values" if d == 0 else "recv_values"]
+        out = {k: np.empty(n, dtype=np.int32) for k in ("index", "bufpos", "stride")}
+        st = self._lib.lg_halo_plan_entries(self._h, d, out["index"].ctypes.data,
+                                            out["bufpos"].ctypes.data, out["stride"].ctypes.data, n)
+        if st:
+            _raise(st, self._lib)
+        return out
+
+    def _ptrs(self, fields):
+        if len(fields) != self.nfields:
+            raise ValueError(f"need {self.nfields} fields")
+        return (ctypes.c_void_p * self.nfields)(*[_dev_ptr(f) for f in fields])
+
+    def pack(self, fields, send_buf, stream=None) -> None:
+        st = self._lib.lg_halo_pack(self._h, self._ptrs(fields), _dev_ptr(send_buf), stream)
+        if st:
+            _raise(st, self._lib)
+
+    def unpack(self, fields, recv_buf, stream=None) -> None:
+        st = self._lib.lg_halo_unpack(self._h, self._ptrs(fields), _dev_ptr(recv_buf), stream)
         if st:
             _raise(st, self._lib)

@@ -40,6 +40,7 @@ CUDA_UNITS = [
     ("lg_peak.cu", ["--fmad=true"]),
     ("lg_noalloc.cu", ["--fmad=false"]),
     ("lg_setup.cu", ["--fmad=false"]),
+    ("lg_halo.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["lg_problem.cc"]
 

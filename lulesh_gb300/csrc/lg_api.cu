@@ -449,6 +449,13 @@ int lg_create(const lg_opts *opts, lg_domain **out)
                          opts->nx, opts->numReg, opts->its);
     if ((long long)opts->nx * opts->nx * opts->nx * 8 > 2147483647LL)
         return set_error(LG_ERR_INVALID, "nx=%d exceeds the 32-bit corner index range", opts->nx);
+    // A negative cost makes a region's EOS repetition count 0 or negative
+    // (lulesh.cc:2390-2400); the reference then stores pressures and energies
+    // its repetition loop never computed (lulesh.cc:2296-2308), so no result
+    // is defined to match.
+    if (opts->cost < 0)
+        return set_error(LG_ERR_INVALID, "cost=%d: the EOS repetition count 1+cost must be "
+                         "positive", opts->cost);
     const lg::KernelSet *ks = nullptr;
     switch (opts->precision) {
     case LG_FP64: ks = lg::kernels_fp64_strict(); break;

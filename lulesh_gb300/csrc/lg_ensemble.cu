@@ -372,6 +372,8 @@ int lg_ensemble_create(int nprob, const lg_opts *opts, lg_ensemble **out)
         const lg_opts &o = opts[i];
         if (o.nx < 1 || o.numReg < 1 || o.its < 0 || (long long)o.nx * o.nx * o.nx * 8 > 2147483647LL)
             return fail(err(LG_ERR_INVALID, "problem %d: invalid size", i));
+        if (o.cost < 0)  // repetition counts 1+cost and 10(1+cost) must be positive
+            return fail(err(LG_ERR_INVALID, "problem %d: cost=%d is negative", i, o.cost));
         // sizes, constants, time state and regions; the mesh and fields are
         // built on the device
         en->prob.push_back(lg::build_sedov_scalars(o.nx, o.numReg, o.balance, o.cost, o.hgcoef,

@@ -208,6 +208,11 @@ extern "C" int lg_calc_force_for_nodes_noalloc(
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double *cs = slot.scratch;
     int *status = reinterpret_cast<int *>(cs + kScratchDoubles);
+    // A launch error left pending by unrelated earlier work of the caller is
+    // not this call's failure: clear it so that the check after the launches
+    // below sees only these kernels.  (A sticky error cannot be cleared; the
+    // status reset then fails and is reported as such.)
+    (void)cudaGetLastError();
     // the status word must start at zero; the corner values are all rewritten
     if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess)
         return fail(LG_ERR_CUDA, "lg_calc_force_for_nodes_noalloc: status reset failed");
@@ -216,11 +221,13 @@ extern "C" int lg_calc_force_for_nodes_noalloc(
         numElem, nodelist, x, y, z, xd, yd, zd, p, q, v, volo, ss, elemMass, hgcoef, cs, status);
     k_gather_static<<<(numNode + kb - 1) / kb, kb, 0, st>>>(
         numElem, numNode, nodeElemStart, nodeElemCornerList, hgcoef > 0., cs, fx, fy, fz);
-    int h_status = 0;
-    if (cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-        return fail(LG_ERR_CUDA, "lg_calc_force_for_nodes_noalloc: kernel launch or sync failed");
     if (cudaGetLastError() != cudaSuccess)
         return fail(LG_ERR_CUDA, "lg_calc_force_for_nodes_noalloc: kernel launch failed");
+    int h_status = 0;
+    if (cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return fail(LG_ERR_CUDA, "lg_calc_force_for_nodes_noalloc: status read-back failed");
+    if (cudaStreamSynchronize(st) != cudaSuccess)
+        return fail(LG_ERR_CUDA,
+                    "lg_calc_force_for_nodes_noalloc: the kernels failed while running");
     return h_status;  // 0, or -1 (VolumeError) as the reference's exit code
 }

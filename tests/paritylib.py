@@ -57,3 +57,25 @@ def normwise_rel_err(gpu: np.ndarray, ref: np.ndarray) -> float:
     scale = float(np.max(np.abs(ref))) if np.size(ref) else 0.0
     d = float(np.max(np.abs(np.asarray(gpu) - np.asarray(ref)))) if np.size(ref) else 0.0
     return d / scale if scale else d
+
+
+def symmetry_deltas(e: np.ndarray, nx: int) -> dict:
+    """Plane-0 symmetry deltas of the energy field, as the reference's
+    end-of-run self-check computes them (lulesh-util.cc:197-212): over
+    j < k < nx, |e[j*nx+k] - e[k*nx+j]|, its maximum and sum, and the largest
+    difference relative to e[k*nx+j]."""
+    j, k = np.triu_indices(nx, 1)
+    a, b = e[j * nx + k], e[k * nx + j]
+    d = np.abs(a - b)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = np.where(d > 0, d / b, 0.0)
+    return {"MaxAbsDiff": float(d.max(initial=0.0)), "TotalAbsDiff": float(d.sum()),
+            "MaxRelDiff": float(np.nanmax(rel, initial=0.0))}
+
+
+def total_energy(state: dict) -> float:
+    """Internal sum(e * volo) plus kinetic sum(m |u|^2) / 2 of a state dict
+    holding e, volo, nodalMass, xd, yd, zd."""
+    ke = 0.5 * np.sum(state["nodalMass"] * (state["xd"] ** 2 + state["yd"] ** 2 +
+                                            state["zd"] ** 2))
+    return float(np.sum(state["e"] * state["volo"]) + ke)

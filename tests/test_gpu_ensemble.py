@@ -1,8 +1,12 @@
 """Batched ensemble: every member must evolve exactly as the same problem run
 alone through lg_create/lg_step (same arithmetic, same order), each with its
-own time step and stop test."""
+own time step and stop test, and must match the oracle run with that
+member's own options (hourglass coefficient lulesh-init.cc:25, deposited
+energy lulesh-init.cc:183-190, regions) within the FP64 bar."""
 import numpy as np
 import pytest
+
+from paritylib import FP64_TOL, compare_states
 
 pytestmark = pytest.mark.gpu
 
@@ -125,3 +129,41 @@ def test_one_member_fails_alone(native_lib):
         assert en.scalar(i, "cycle") == clean.scalar(i, "cycle")
         for f in ("e", "x", "xd"):
             assert np.array_equal(_bits(en.field(i, f)), _bits(clean.field(i, f))), (i, f)
+
+
+_ORACLE_MEMBERS = {}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64-fma"])
+def test_sampled_members_match_oracle(native_lib, oracle_built, precision, capsys):
+    """The first 12 members of the ensemble study's seed-0 set (s in 16..64,
+    hgcoef in [1, 3], energy factor in [0.5, 2], 4..16 regions), 100 cycles
+    in one batched run, each against the oracle built with the member's own
+    options: every field within 1e-10."""
+    import lulesh_gb300 as lg
+    from oracle.oracle import OracleDomain
+    members = lg.sample_ensemble(12, seed=0)
+    for m in members:
+        m["its"] = 100
+    en = lg.Ensemble(members, precision=precision)
+    assert en.step(100) == 0
+    fields = lg.NODE_FIELDS + lg.ELEM_FIELDS
+    worst_all = 0.0
+    for i, m in enumerate(members):
+        key = tuple(sorted(m.items()))
+        if key not in _ORACLE_MEMBERS:
+            o = OracleDomain(m["nx"], m["numReg"], m["balance"], m["cost"], m["hgcoef"],
+                             m["einit_factor"])
+            assert o.step(100) == 0
+            _ORACLE_MEMBERS[key] = o.state()
+            o.close()
+        ref = _ORACLE_MEMBERS[key]
+        assert en.scalar(i, "cycle") == ref["cycle"] == 100
+        errs = compare_states({f: en.field(i, f) for f in fields}, ref, fields)
+        worst = max(errs, key=errs.get)
+        worst_all = max(worst_all, errs[worst])
+        with capsys.disabled():
+            print(f"\n[ensemble-vs-oracle] {precision} member {i}: s={m['nx']} "
+                  f"r{m['numReg']} hg {m['hgcoef']:.3f} energy x{m['einit_factor']:.3f}: "
+                  f"worst {worst} = {errs[worst]:.3e}")
+        assert errs[worst] <= FP64_TOL, (i, errs)

@@ -97,6 +97,12 @@ def test_invalid_options_rejected(native_lib):
         lg.Domain(0, device=-1)
     with pytest.raises(lg.LuleshError):
         lg.Domain(4, numReg=0, device=-1)
+    # a negative cost leaves regions with no EOS repetitions, for which the
+    # reference stores values it never computed: rejected, not guessed
+    for cost in (-1, -5):
+        with pytest.raises(lg.LuleshError, match="cost"):
+            lg.Domain(4, cost=cost, device=-1)
+    lg.Domain(4, cost=0, device=-1).close()   # repetitions 1 and 10: valid
 
 
 def _cli():
@@ -145,3 +151,17 @@ def test_material_work_items(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout[-3000:]
     assert r.stdout.strip().endswith("failed checks 0"), r.stdout[-3000:]
+
+
+def test_domain_sync_binding_compiles_against_reference_header(oracle_built):
+    """tests/binding_domain_sync.cc (the field-sync pattern of the integration
+    guide, with its name -> Domain_member table) compiles against the
+    reference's own lulesh.h.  Runs where the reference sources were present
+    when the oracle was built."""
+    if not oracle_built.ref_available():
+        pytest.skip("reference sources not available on this host")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run(["make", "-s", "-C", os.path.join(root, "oracle"), "binding"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "skipping" not in r.stdout
