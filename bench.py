@@ -67,35 +67,43 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
     }.get(kernel, 160 + 104 * n_over_e)
 
 
-# FP64 thread-instructions (DADD + DMUL + DFMA) per element per launch,
-# from an ncu capture of the four cycle kernels at cycle 170 of the
-# reference problem: s=100, 11 regions for the strict and the FMA builds;
-# s=96, 16 regions, balance 2, cost 4 for the mixed build (k_nodes: counted
-# per node, stored per element at that mesh's N/E; k_material: that region
-# mix).
-FP64_INST_PER_ELEM = {
-    "fp64": {"k_forces": 1321, "k_kinematics": 699, "k_material": 783,
-             "k_nodes": 73.6 * 1030301 / 1000000},
-    "fp64-fma": {"k_forces": 828, "k_kinematics": 601, "k_material": 724,
-                 "k_nodes": 67.6 * 1030301 / 1000000},
-    "mixed": {"k_forces": 22, "k_kinematics": 94, "k_material": 576,
-              "k_nodes": 12.0 * 912673 / 884736},
+# FP64 pipe lane slots per unit per launch: warp instructions issued to the
+# FP64 pipe (smsp__inst_executed_pipe_fp64, every lane counted whether active
+# or not, since a warp instruction holds the pipe for the same time either
+# way) x 32 / units (elements; k_nodes: nodes), from ncu captures of the four
+# cycle kernels of the benchmark problem (s=150, 11 regions, balance 1, cost
+# 1) at cycle 10; captures at cycles 1 to 500 agree to 0.5 %
+# (profiles/leapfrog_fp64_s150_counts.md).  The mixed build's counts are from
+# s=192, 16 regions, balance 2, cost 4 at cycle 10.
+FP64_SLOTS_PER_UNIT = {
+    "fp64": {"k_forces": 1273, "k_nodes": 78, "k_kinematics": 700, "k_material": 860},
+    "fp64-fma": {"k_forces": 785, "k_nodes": 72, "k_kinematics": 602, "k_material": 804},
+    "mixed": {"k_forces": 71, "k_nodes": 12, "k_kinematics": 120, "k_material": 607},
 }
-# The region mix (regions, balance, cost) each build's k_material count was
-# taken with; the EOS repetitions make that count depend on it.
-FP64_INST_REGION_MIX = {"fp64": (11, 1, 1), "fp64-fma": (11, 1, 1), "mixed": (16, 2, 4)}
+# The workload (nx, regions, balance, cost) each build's counts were taken
+# with; k_material's depend on the region mix, the others on nothing.
+FP64_SLOTS_WORKLOAD = {"fp64": (150, 11, 1, 1), "fp64-fma": (150, 11, 1, 1),
+                       "mixed": (192, 16, 2, 4)}
+# One FP64 warp instruction per 16 cycles per SM on GB300 (ncu's
+# sm__pipe_fp64_cycles_active peak): 2 lanes per SM per cycle.
+FP64_LANES_PER_SM_CYCLE = 2.0
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element per
-# launch (k_nodes: per node), from the same ncu captures, scaled to the
-# benchmarked mesh by the units it processes.  Well above the algorithmic
-# bytes: the per-corner force scratch (k_forces writes, k_nodes reads) and
-# the region-order gathers of k_material.
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit per
+# launch (elements; k_nodes: nodes): the FP64 builds from the s=150
+# captures above (the benchmark mesh itself, cycle 10; cycle 500 agrees to
+# 0.1 %), the mixed build from s=96, 16 regions, balance 2, cost 4, scaled
+# by the units a launch processes.  Well above the algorithmic bytes: the
+# per-corner force scratch (k_forces writes it, k_nodes reads it) and the
+# region-order gathers of k_material.
 TRAFFIC_PER_UNIT = {
-    "fp64": {"k_forces": 456.8, "k_nodes": 550.9, "k_kinematics": 140.3, "k_material": 210.5},
-    "fp64-fma": {"k_forces": 456.2, "k_nodes": 550.3, "k_kinematics": 140.4, "k_material": 210.9},
+    "fp64": {"k_forces": 496.0, "k_nodes": 568.3, "k_kinematics": 166.6, "k_material": 291.3},
+    "fp64-fma": {"k_forces": 496.0, "k_nodes": 567.8, "k_kinematics": 166.9, "k_material": 291.8},
     "mixed": {"k_forces": 264.4, "k_nodes": 337.7, "k_kinematics": 120.6, "k_material": 162.6},
 }
+TRAFFIC_SOURCE = {"fp64": "ncu DRAM bytes of the s=150 benchmark mesh (cycle 10)",
+                  "fp64-fma": "ncu DRAM bytes of the s=150 benchmark mesh (cycle 10)",
+                  "mixed": "ncu DRAM bytes per unit at s=96, scaled to the mesh"}
 
 
 def _peaks() -> dict:
@@ -551,23 +559,35 @@ def run_gpu(a):
     traffic = None if per_unit is None else per_unit * (N if dom == "k_nodes" else E)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
-                "traffic_source": "ncu DRAM bytes per unit on a smaller mesh, scaled"
-                if traffic else None, "kernel": dom,
+                "traffic_source": TRAFFIC_SOURCE.get(a.precision) if traffic else None,
+                "kernel": dom,
                 "peak_source": peaks["src"], "alg_bytes_per_launch": ab,
                 "kernel_ms_per_launch": avg_ms,
                 "kernel_share": {k: v / total for k, v in prof.items()}}
     # FP64 pipe roofline (the bound of this path)
-    fp64_peak = lg.measure_pipe("fma")
-    per_elem = FP64_INST_PER_ELEM.get(a.precision, {}).get(dom)
-    if dom == "k_material" and FP64_INST_REGION_MIX.get(a.precision) != (a.regions, a.balance,
-                                                                         a.cost):
-        per_elem = None  # counted with another region mix
-    roof64 = {"bound": "fp64_pipe", "peak_ginst_per_s": fp64_peak, "unit": "G FP64 inst/s",
-              "kernel": dom}
-    if per_elem:
-        ach = per_elem * E / (avg_ms * 1e-3) / 1e9
-        roof64.update({"achieved": ach, "frac": ach / fp64_peak,
-                       "inst_per_elem": per_elem})
+    # FP64 pipe roofline (the bound of this path): the dominant kernel's pipe
+    # lane slots per launch over its time, against the pipe's issue rate at
+    # the SM clock sampled during the timed region; the DFMA
+    # microbenchmark's rate is reported beside it
+    import torch
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    clk_sum = clk.summary() or {}
+    sm_hz = (clk_sum.get("sm_mhz") or 2070.0) * 1e6
+    pipe_peak = FP64_LANES_PER_SM_CYCLE * sms * sm_hz / 1e9
+    slots = FP64_SLOTS_PER_UNIT.get(a.precision, {})
+    roof64 = {"bound": "fp64_pipe", "unit": "G FP64 lane-inst/s", "kernel": dom,
+              "peak": pipe_peak, "peak_source": f"2 lanes/SM/cycle x {sms} SMs x "
+                                                f"{sm_hz / 1e6:.0f} MHz (sampled)",
+              "dfma_microbenchmark": lg.measure_pipe("fma")}
+    if FP64_SLOTS_WORKLOAD.get(a.precision) == (a.nx, a.regions, a.balance, a.cost) and slots:
+        per_unit = slots.get(dom)
+        units = N if dom == "k_nodes" else E
+        ach = per_unit * units / (avg_ms * 1e-3) / 1e9
+        cyc_slots = sum(slots[k] * (N / E if k == "k_nodes" else 1.0) for k in slots)
+        cyc_ach = cyc_slots * E * a.steps / (ms_max * 1e-3) / 1e9
+        roof64.update({"achieved": ach, "frac": ach / pipe_peak, "slots_per_unit": per_unit,
+                       "cycle_slots_per_elem": cyc_slots, "cycle_achieved": cyc_ach,
+                       "cycle_frac": cyc_ach / pipe_peak})
 
     # end to end through the C ABI with host buffers
     fields = lg.NODE_FIELDS + lg.ELEM_FIELDS

@@ -160,10 +160,17 @@ int upload_regions(lg_domain *d)
     if ((long long)perm.size() > d->item_cap)
         return set_error(LG_ERR_STATE, "%zu work items exceed the capacity %d", perm.size(),
                          d->item_cap);
+    std::vector<int> slot_elem, item_slot;
+    lg::build_item_slots(perm, 128, slot_elem, item_slot);
     int st;
     if ((st = upload(d, d->ds.regNumList, p.regNumList))) return st;
     if ((st = upload(d, d->ds.regPerm, perm))) return st;
     if ((st = upload(d, d->ds.regRep, rep))) return st;
+    if ((st = upload(d, d->ds.slotElem, slot_elem))) return st;
+    if ((st = upload(d, d->ds.itemSlot, item_slot))) return st;
+    // the graphs hold the kernel arguments (nItems) and the material kernel
+    // chosen for them
+    if (d->ds.nItems != (int)perm.size()) drop_graphs(d);
     d->ds.nItems = (int)perm.size();
     LG_CUDA(cudaStreamSynchronize(d->stream));
     return LG_OK;
@@ -440,6 +447,31 @@ void lg_default_opts(lg_opts *o)
     o->device = 0;
 }
 
+// Block size of a one-thread-per-unit kernel over `units` threads.  Every
+// FP64 warp instruction holds an SM's FP64 pipe for the same time, so a
+// kernel lasts about as long as its busiest SM's warps take: blocks spread
+// over the SMs, the busiest gets ceil(blocks / SMs) of them.  Smaller blocks
+// are taken when they cut that warp count by more than 3 %, which happens on
+// small meshes only (s=30: 8 warps with blocks of 128, 6 with 64); results
+// do not depend on the block size.
+static int pick_block(long long units, int sms)
+{
+    auto busiest = [&](int bs) {
+        const long long blocks = (units + bs - 1) / bs;
+        return (double)((blocks + sms - 1) / sms) * (bs / 32);
+    };
+    int best = 128;
+    double best_cost = busiest(128);
+    for (const int bs : {64, 32}) {
+        const double c = busiest(bs);
+        if (c < 0.97 * best_cost) {
+            best = bs;
+            best_cost = c;
+        }
+    }
+    return best;
+}
+
 int lg_create(const lg_opts *opts, lg_domain **out)
 {
     if (!opts || !out) return set_error(LG_ERR_INVALID, "null argument");
@@ -511,7 +543,8 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     size_t o_conn[7];
     for (auto &o : o_conn) o = L.add<int>(E);
     const size_t o_regnum = L.add<int>(E), o_perm = L.add<int>(d->item_cap),
-                 o_rep = L.add<int>(d->item_cap);
+                 o_rep = L.add<int>(d->item_cap), o_slot = L.add<int>((size_t)eblocks * 128),
+                 o_islot = L.add<int>(d->item_cap);
     const size_t o_nes = L.add<int>(N + 1), o_ncl = L.add<int>(8 * E);
     const size_t o_symm = L.add<uint8_t>(N);
     const size_t o_part = L.add<double>(2 * (size_t)eblocks);
@@ -545,11 +578,15 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     s.regNumList = reinterpret_cast<int *>(base + o_regnum);
     s.regPerm = reinterpret_cast<int *>(base + o_perm);
     s.regRep = reinterpret_cast<int *>(base + o_rep);
+    s.slotElem = reinterpret_cast<int *>(base + o_slot);
+    s.itemSlot = reinterpret_cast<int *>(base + o_islot);
     s.nodeElemStart = reinterpret_cast<int *>(base + o_nes);
     s.nodeElemCornerList = reinterpret_cast<int *>(base + o_ncl);
     s.symm = reinterpret_cast<uint8_t *>(base + o_symm);
     s.dt_partial = reinterpret_cast<double *>(base + o_part);
     s.dt_blocks = eblocks;
+    s.bs_elem = pick_block((long long)E, sms);
+    s.bs_node = pick_block((long long)N, sms);
     s.ctl = reinterpret_cast<lg::Ctl *>(base + o_ctl);
     s.prm = make_params(p.k);
 

@@ -163,6 +163,13 @@ struct IeeeOps {
     static __device__ __forceinline__ bool le(double a, double b) { return dle(a, b); }
     // |a| < b for b >= +0
     static __device__ __forceinline__ bool abs_lt(double a, double b) { return dabs_lt(a, b); }
+    // the sound-speed numerator of CalcSoundSpeedForElems (lulesh.cc:2190),
+    // in the reference's operation order (contracted only by the FMA build)
+    static __device__ __forceinline__ double ss_num(double pbvc, double e, double v, double bvc,
+                                                    double p)
+    {
+        return pbvc * e + v * v * bvc * p;
+    }
 };
 
 // sound-speed term of lulesh.cc:2083-2090, 2126-2133, 2158-2165, 2190-2197
@@ -197,14 +204,20 @@ __device__ __forceinline__ double pressure(const Params &P, double &bvc, double 
     return p_new;
 }
 
-// EvalEOSForElems for one element (lulesh.cc:2204-2324) with
-// CalcEnergyForElems (2048-2176) and CalcSoundSpeedForElems (2180-2200).
-// All rep repetitions are evaluated, as in the reference.
+// The results of an element's EOS repetitions: the last repetition's
+// pressure, energy and viscosity, and the bulk-viscosity terms bvc, pbvc the
+// sound speed is computed from.
+struct EosOut {
+    double p, e, q, bvc, pbvc;
+};
+
+// The rep repetitions of CalcEnergyForElems (lulesh.cc:2048-2176) with
+// CalcPressureForElems (2014-2044), as EvalEOSForElems runs them for one
+// element (2204-2324).  Every repetition is evaluated, as in the reference.
 template <class M = IeeeOps>
-__device__ __forceinline__ void eval_eos(const Params &P, double e_in, double delv_in,
-                                         double p_in, double q_in, double qq_in, double ql_in,
-                                         double vnewc, int rep, double &p_out, double &e_out,
-                                         double &q_out, double &ss_out, bool need_ss = true)
+__device__ __forceinline__ EosOut eos_reps(const Params &P, double e_in, double delv_in,
+                                           double p_in, double q_in, double qq_in,
+                                           double ql_in, double vnewc, int rep)
 {
     const double rho0 = P.refdens;
     double p_new = 0., e_new = 0., q_new = 0., bvc = 0., pbvc = 0.;
@@ -264,10 +277,29 @@ __device__ __forceinline__ void eval_eos(const Params &P, double e_in, double de
             if (M::abs_lt(q_new, P.q_cut)) q_new = 0.;
         }
     }
-    p_out = p_new;
-    e_out = e_new;
-    q_out = q_new;
-    ss_out = need_ss ? ssc_of<M>(pbvc * e_new + vnewc * vnewc * bvc * p_new, rho0) : 0.0;
+    return {p_new, e_new, q_new, bvc, pbvc};
+}
+
+// CalcSoundSpeedForElems for one element (lulesh.cc:2180-2200).
+template <class M = IeeeOps>
+__device__ __forceinline__ double eos_sound_speed(const Params &P, const EosOut &o, double vnewc)
+{
+    return ssc_of<M>(M::ss_num(o.pbvc, o.e, vnewc, o.bvc, o.p), P.refdens);
+}
+
+// EvalEOSForElems for one element (lulesh.cc:2204-2324): the repetitions,
+// then the sound speed when need_ss.
+template <class M = IeeeOps>
+__device__ __forceinline__ void eval_eos(const Params &P, double e_in, double delv_in,
+                                         double p_in, double q_in, double qq_in, double ql_in,
+                                         double vnewc, int rep, double &p_out, double &e_out,
+                                         double &q_out, double &ss_out, bool need_ss = true)
+{
+    const EosOut o = eos_reps<M>(P, e_in, delv_in, p_in, q_in, qq_in, ql_in, vnewc, rep);
+    p_out = o.p;
+    e_out = o.e;
+    q_out = o.q;
+    ss_out = need_ss ? eos_sound_speed<M>(P, o, vnewc) : 0.0;
 }
 
 __device__ __forceinline__ double dmin_sel(double a, double b) { return (b < a) ? b : a; }

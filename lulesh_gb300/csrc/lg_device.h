@@ -77,6 +77,13 @@ struct DevState {
     // each with a share of the EOS repetitions; the element's last one is its
     // writer, regRep > 0; padding has regPerm < 0).  Ensembles: nItems = E.
     int nItems;
+    // the shared-item path's slots (lg::build_item_slots): per block of 128
+    // items its distinct elements, and per item its element's slot
+    int *slotElem, *itemSlot;
+    // block sizes of the single-problem element kernels (k_forces,
+    // k_kinematics) and of k_nodes: 32, 64 or 128 (0 means 128), chosen at
+    // creation so that small meshes spread evenly over the SMs
+    int bs_elem, bs_node;
     // per-corner force scratch, 6 * 8 * E doubles
     double *corner;
     // per-block minima of the time-constraint reduction

@@ -19,24 +19,28 @@
 namespace lg {
 namespace fast {
 
-// double -> float by re-biasing the exponent and truncating the mantissa
-// (round toward zero); values below the float normal range become zero,
+// double -> float, rounded to nearest (ties to even), on the integer pipe:
+// the magnitude's bits re-biased from the double to the float exponent, then
+// rounded on their 29 dropped bits by one 64-bit add (half an ulp less one,
+// plus the kept mantissa's lowest bit, which turns exact ties to even); a
+// carry out of the mantissa steps the exponent, and from the largest finite
+// float to infinity.  Values below the float normal range become zero,
 // values above it infinity.
 __device__ __forceinline__ float to_f32(double v)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned sign = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-    const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    // exponent - 1023 + 127 <= 0 (the magnitude's top bits below 897 << 52)
+    const long long t = (long long)((b & 0x7fffffffffffffffull) - (896ull << 52));
     unsigned r;
-    if (e <= 0)
-        r = sign;
-    else if (e >= 255)
-        r = sign | 0x7f800000u;
-    else
-        r = sign | ((unsigned)e << 23) | mant;
-    return __uint_as_float(r);
+    if (t < (1ll << 52)) {
+        r = 0u;
+    } else {
+        const unsigned long long q =
+            ((unsigned long long)t + 0x0fffffffull + (((unsigned long long)t >> 29) & 1ull)) >> 29;
+        r = q >= 0x7f800000ull ? 0x7f800000u : (unsigned)q;
+    }
+    return __uint_as_float(sign | r);
 }
 
 // float -> double, exact for normal values (float subnormals become zero).
@@ -101,6 +105,14 @@ struct FastOps {
     {
         return ((unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull) <
                (unsigned long long)__double_as_longlong(b);
+    }
+    // the sound-speed numerator pbvc e + v^2 bvc p with its roundings fixed,
+    // so every kernel that evaluates it (the fused per-element path and the
+    // shared-item path) gets the same bits whatever the compiler contracts
+    static __device__ __forceinline__ double ss_num(double pbvc, double e, double v, double bvc,
+                                                    double p)
+    {
+        return __fma_rn(pbvc, e, __dmul_rn(__dmul_rn(__dmul_rn(v, v), bvc), p));
     }
 };
 

@@ -10,10 +10,13 @@
 
 #ifdef __CUDACC__
 #include <cuda_runtime.h>
+#include <cstring>
 #define LG_HD __host__ __device__ __forceinline__
 #else
 #include <cmath>
+#include <cstring>
 #define LG_HD inline
+#include <math.h>
 using std::sqrt;
 #endif
 
@@ -61,6 +64,88 @@ LG_HD R jacobian_det(const R *x, const R *y, const R *z)
     const R cjyet = (fjxxi * fjzze) - (fjzxi * fjxze);
     const R cjzet = -(fjxxi * fjyze) + (fjyxi * fjxze);
     return R(0.015625) * (fjxet * cjxet + fjyet * cjyet + fjzet * cjzet);
+}
+
+// Bits of a double, and a float from its bits, on host and device.
+LG_HD unsigned long long bits_of(double v)
+{
+#ifdef __CUDA_ARCH__
+    return (unsigned long long)__double_as_longlong(v);
+#else
+    unsigned long long b;
+    std::memcpy(&b, &v, sizeof b);
+    return b;
+#endif
+}
+LG_HD float float_of(unsigned u)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    std::memcpy(&f, &u, sizeof f);
+    return f;
+#endif
+}
+
+// double -> float toward zero by re-biasing the exponent on the integer pipe
+// (off GB300's FP64 pipe): |error| <= 2^-23 |v|; magnitudes below 2^-126
+// become zero, above the float range infinity.
+LG_HD float f32_trunc(double v)
+{
+    const unsigned long long b = bits_of(v);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0) return float_of(sign);
+    if (e >= 255) return float_of(sign | 0x7f800000u);
+    return float_of(sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+
+// True when jacobian_det(x, y, z) in FP64 is certainly positive, decided in
+// FP32 with an a-priori error bound; false means "evaluate it in FP64".  The
+// reference uses that determinant only for its sign (the VolumeError test of
+// CalcVolumeForceForElems, lulesh.cc:1082-1091), so the filter changes no
+// result.  Bound, with u = 2^-24 and X the largest coordinate magnitude:
+//   * each converted coordinate is off by at most 2u X (+ 2^-126 flushed);
+//     each of the nine sums fj (7 roundings of partial sums bounded by 8X)
+//     is then off by at most Delta = 80 u X + 2^-120;
+//   * the determinant is a sum of six signed triple products of the fj, so
+//     input errors move it by at most 18 G^2 Delta (G = max |fj| + Delta),
+//     and its FP32 evaluation (with or without contraction) adds at most
+//     32 u G^3;
+// twice that bound, times the 2^-6 scale, is compared with the FP32 value.
+// The FP64 value's own error (~1e-16 relative) is far inside the factor 2.
+// NaN or out-of-range inputs give false.
+LG_HD bool jacobian_certainly_positive(const double *x, const double *y, const double *z)
+{
+    float xf[8], yf[8], zf[8];
+    float X = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        xf[j] = f32_trunc(x[j]);
+        yf[j] = f32_trunc(y[j]);
+        zf[j] = f32_trunc(z[j]);
+        X = fmaxf(X, fmaxf(fabsf(xf[j]), fmaxf(fabsf(yf[j]), fabsf(zf[j]))));
+    }
+    const float a = jacobian_det(xf, yf, zf);  // includes the 2^-6 scale
+    const float fx0 = (xf[6] - xf[0]) + (xf[5] - xf[3]) - (xf[7] - xf[1]) - (xf[4] - xf[2]);
+    const float fx1 = (xf[6] - xf[0]) - (xf[5] - xf[3]) + (xf[7] - xf[1]) - (xf[4] - xf[2]);
+    const float fx2 = (xf[6] - xf[0]) + (xf[5] - xf[3]) + (xf[7] - xf[1]) + (xf[4] - xf[2]);
+    const float fy0 = (yf[6] - yf[0]) + (yf[5] - yf[3]) - (yf[7] - yf[1]) - (yf[4] - yf[2]);
+    const float fy1 = (yf[6] - yf[0]) - (yf[5] - yf[3]) + (yf[7] - yf[1]) - (yf[4] - yf[2]);
+    const float fy2 = (yf[6] - yf[0]) + (yf[5] - yf[3]) + (yf[7] - yf[1]) + (yf[4] - yf[2]);
+    const float fz0 = (zf[6] - zf[0]) + (zf[5] - zf[3]) - (zf[7] - zf[1]) - (zf[4] - zf[2]);
+    const float fz1 = (zf[6] - zf[0]) - (zf[5] - zf[3]) + (zf[7] - zf[1]) - (zf[4] - zf[2]);
+    const float fz2 = (zf[6] - zf[0]) + (zf[5] - zf[3]) + (zf[7] - zf[1]) + (zf[4] - zf[2]);
+    const float F = fmaxf(fmaxf(fmaxf(fabsf(fx0), fabsf(fx1)), fmaxf(fabsf(fx2), fabsf(fy0))),
+                          fmaxf(fmaxf(fabsf(fy1), fabsf(fy2)),
+                                fmaxf(fabsf(fz0), fmaxf(fabsf(fz1), fabsf(fz2)))));
+    const float u = 5.9604645e-8f;  // 2^-24
+    const float delta = 80.f * u * X + 7.5231638e-37f;  // + 2^-120
+    const float G = F + delta;
+    const float bound = 2.f * 0.015625f * (18.f * G * G * delta + 32.f * u * G * G * G);
+    return a > bound;  // false for NaN
 }
 
 // CalcElemShapeFunctionDerivatives rows 0..3 of B (rows 4..7 are their

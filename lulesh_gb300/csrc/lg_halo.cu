@@ -366,12 +366,13 @@ int lg_halo_plan_entries(const lg_halo_plan *p, int dir, int *index, int *bufpos
 
 int lg_halo_pack(lg_halo_plan *p, double *const *fields, double *send_buf, void *stream)
 {
-    if (!p || !send_buf) return fail(LG_ERR_INVALID, "lg_halo_pack: null argument");
+    if (!p) return fail(LG_ERR_INVALID, "lg_halo_pack: null plan");
+    const int n = p->info.send_values;
+    if (n == 0) return LG_OK;  // no neighbour (tp = 1): nothing to pack
+    if (!send_buf) return fail(LG_ERR_INVALID, "lg_halo_pack: null buffer");
     Fields fl;
     int st;
     if ((st = get_fields(p, fields, fl)) || (st = ensure_device(p))) return st;
-    const int n = p->info.send_values;
-    if (n == 0) return LG_OK;
     (void)cudaGetLastError();
     k_halo_pack<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
         n, p->nfields, fl, p->d_s_index, p->d_s_pos, p->d_s_stride, send_buf);
@@ -381,12 +382,13 @@ int lg_halo_pack(lg_halo_plan *p, double *const *fields, double *send_buf, void 
 
 int lg_halo_unpack(lg_halo_plan *p, double *const *fields, const double *recv_buf, void *stream)
 {
-    if (!p || !recv_buf) return fail(LG_ERR_INVALID, "lg_halo_unpack: null argument");
+    if (!p) return fail(LG_ERR_INVALID, "lg_halo_unpack: null plan");
+    const int nt = p->info.recv_targets;
+    if (nt == 0) return LG_OK;  // no neighbour: nothing received
+    if (!recv_buf) return fail(LG_ERR_INVALID, "lg_halo_unpack: null buffer");
     Fields fl;
     int st;
     if ((st = get_fields(p, fields, fl)) || (st = ensure_device(p))) return st;
-    const int nt = p->info.recv_targets;
-    if (nt == 0) return LG_OK;
     (void)cudaGetLastError();
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int grid = (nt + 255) / 256;

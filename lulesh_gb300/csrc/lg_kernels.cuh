@@ -84,7 +84,6 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
     // InitStressTermsForElems (273-286) + IntegrateStressForElems (494-587)
     {
         const double sig = -s.p[k] - s.q[k];
-        const double determ = jacobian_det(x, y, z);
         double pfx[8], pfy[8], pfz[8];
 #if LG_REASSOC
         node_normals_nozero(pfx, pfy, pfz, x, y, z);
@@ -97,7 +96,13 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
             cs[1 * E8 + (size_t)j * E + k] = -(sig * pfy[j]);
             cs[2 * E8 + (size_t)j * E + k] = -(sig * pfz[j]);
         }
-        if (determ <= 0.0) raise_status(ctl, -1);  // lulesh.cc:1082-1091
+        // lulesh.cc:1082-1091 uses the Jacobian determinant only for its
+        // sign: an FP32 filter with a rigorous error bound settles it, and
+        // the FP64 determinant is evaluated only in a warp with an element
+        // the filter cannot settle (none on a valid mesh)
+        const bool sure = jacobian_certainly_positive(x, y, z);
+        if (__any_sync(__activemask(), !sure) && !sure && jacobian_det(x, y, z) <= 0.0)
+            raise_status(ctl, -1);
     }
 
     // CalcHourglassControlForElems (995-1057)
@@ -364,104 +369,105 @@ struct MatItem {
     double qlin, qquad, q_old, vnewc, vnew, e, delv, p;
 };
 
-// Phase 1, reads only: monotonic-Q limiter, qstop check and the material
-// clamps of item t (MODE != 1).  False for padding.
+// The element part of phase 1, reads only: monotonic-Q limiter, qstop check
+// and the material clamps of element ielem.
+__device__ __forceinline__ void material_inputs(const DevState &s, const int ielem, Ctl *ctl,
+                                                MatItem &m)
+{
+    const Params &P = s.prm;
+    // CalcMonotonicQRegionForElems, lulesh.cc:1761-1921
+    const int bc = s.elemBC[ielem];
+    const double phixi = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_xi, ielem, bc, XI_M_SYMM, XI_M_FREE,
+                                   XI_M, XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
+                                   s.lxip[ielem]);
+    const double phieta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_eta, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
+                                    ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P,
+                                    s.letam[ielem], s.letap[ielem]);
+    const double phizeta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_zeta, ielem, bc, ZETA_M_SYMM,
+                                     ZETA_M_FREE, ZETA_M, ZETA_P_SYMM, ZETA_P_FREE,
+                                     ZETA_P, s.lzetam[ielem], s.lzetap[ielem]);
+    const double vnew = s.vnew[ielem];
+    const double vdov = s.vdov[ielem];
+    double qlin, qquad;
+    if (dlt(0., vdov)) {
+        qlin = 0.;
+        qquad = 0.;
+    } else {
+        double delvxxi = s.delv_xi[ielem] * s.delx_xi[ielem];
+        double delvxeta = s.delv_eta[ielem] * s.delx_eta[ielem];
+        double delvxzeta = s.delv_zeta[ielem] * s.delx_zeta[ielem];
+        if (dlt(0., delvxxi)) delvxxi = 0.;
+        if (dlt(0., delvxeta)) delvxeta = 0.;
+        if (dlt(0., delvxzeta)) delvxzeta = 0.;
+        const double rho = s.elemMass[ielem] / (s.volo[ielem] * vnew);
+        qlin = -P.qlc_monoq * rho *
+               (delvxxi * (1. - phixi) + delvxeta * (1. - phieta) +
+                delvxzeta * (1. - phizeta));
+        qquad = P.qqc_monoq * rho *
+                (delvxxi * delvxxi * (1. - phixi * phixi) +
+                 delvxeta * delvxeta * (1. - phieta * phieta) +
+                 delvxzeta * delvxzeta * (1. - phizeta * phizeta));
+    }
+    m.qlin = qlin;
+    m.qquad = qquad;
+
+    // qstop check on the previous cycle's q, lulesh.cc:1993-2008
+    m.q_old = s.q[ielem];
+    if (dlt(P.qstop, m.q_old)) ctl->err_qstop = 1;
+
+    // ApplyMaterialPropertiesForElems, lulesh.cc:2328-2406
+    double vnewc = vnew;
+    if (dnz(P.eosvmin) && dlt(vnewc, P.eosvmin)) vnewc = P.eosvmin;
+    if (dnz(P.eosvmax) && dlt(P.eosvmax, vnewc)) vnewc = P.eosvmax;
+    double vc = s.v[ielem];
+    if (dnz(P.eosvmin) && dlt(vc, P.eosvmin)) vc = P.eosvmin;
+    if (dnz(P.eosvmax) && dlt(P.eosvmax, vc)) vc = P.eosvmax;
+    if (dle(vc, 0.)) ctl->err_matvol = 1;
+    m.vnewc = vnewc;
+    m.vnew = vnew;
+    m.e = s.e[ielem];
+    m.delv = s.delv[ielem];
+    m.p = s.p[ielem];
+}
+
+// Phase 1 of item t: its element, repetitions and role, and (MODE != 1) the
+// element's inputs.  False for padding.
 template <int MODE>
 __device__ __forceinline__ bool material_load(const DevState &s, const int t, Ctl *ctl,
                                               MatItem &m)
 {
-    const Params &P = s.prm;
     const int ielem = s.regPerm[t];
     if (ielem < 0) return false;
     const int r = s.regRep[t];
     m.ielem = ielem;
     m.writer = r > 0;
     m.reps = r > 0 ? r : -r;
-    if (MODE != 1) {
-        // CalcMonotonicQRegionForElems, lulesh.cc:1761-1921
-        const int bc = s.elemBC[ielem];
-        const double phixi = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_xi, ielem, bc, XI_M_SYMM, XI_M_FREE,
-                                       XI_M, XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
-                                       s.lxip[ielem]);
-        const double phieta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_eta, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
-                                        ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P,
-                                        s.letam[ielem], s.letap[ielem]);
-        const double phizeta = monoq_phi(P.monoq_limiter_mult, P.monoq_max_slope, s.delv_zeta, ielem, bc, ZETA_M_SYMM,
-                                         ZETA_M_FREE, ZETA_M, ZETA_P_SYMM, ZETA_P_FREE,
-                                         ZETA_P, s.lzetam[ielem], s.lzetap[ielem]);
-        const double vnew = s.vnew[ielem];
-        const double vdov = s.vdov[ielem];
-        double qlin, qquad;
-        if (dlt(0., vdov)) {
-            qlin = 0.;
-            qquad = 0.;
-        } else {
-            double delvxxi = s.delv_xi[ielem] * s.delx_xi[ielem];
-            double delvxeta = s.delv_eta[ielem] * s.delx_eta[ielem];
-            double delvxzeta = s.delv_zeta[ielem] * s.delx_zeta[ielem];
-            if (dlt(0., delvxxi)) delvxxi = 0.;
-            if (dlt(0., delvxeta)) delvxeta = 0.;
-            if (dlt(0., delvxzeta)) delvxzeta = 0.;
-            const double rho = s.elemMass[ielem] / (s.volo[ielem] * vnew);
-            qlin = -P.qlc_monoq * rho *
-                   (delvxxi * (1. - phixi) + delvxeta * (1. - phieta) +
-                    delvxzeta * (1. - phizeta));
-            qquad = P.qqc_monoq * rho *
-                    (delvxxi * delvxxi * (1. - phixi * phixi) +
-                     delvxeta * delvxeta * (1. - phieta * phieta) +
-                     delvxzeta * delvxzeta * (1. - phizeta * phizeta));
-        }
-        m.qlin = qlin;
-        m.qquad = qquad;
-
-        // qstop check on the previous cycle's q, lulesh.cc:1993-2008
-        m.q_old = s.q[ielem];
-        if (dlt(P.qstop, m.q_old)) ctl->err_qstop = 1;
-
-        // ApplyMaterialPropertiesForElems, lulesh.cc:2328-2406
-        double vnewc = vnew;
-        if (dnz(P.eosvmin) && dlt(vnewc, P.eosvmin)) vnewc = P.eosvmin;
-        if (dnz(P.eosvmax) && dlt(P.eosvmax, vnewc)) vnewc = P.eosvmax;
-        double vc = s.v[ielem];
-        if (dnz(P.eosvmin) && dlt(vc, P.eosvmin)) vc = P.eosvmin;
-        if (dnz(P.eosvmax) && dlt(P.eosvmax, vc)) vc = P.eosvmax;
-        if (dle(vc, 0.)) ctl->err_matvol = 1;
-        m.vnewc = vnewc;
-        m.vnew = vnew;
-        m.e = s.e[ielem];
-        m.delv = s.delv[ielem];
-        m.p = s.p[ielem];
-    }
+    if (MODE != 1) material_inputs(s, ielem, ctl, m);
     return true;
 }
 
-// Phase 2: the item's EOS repetitions (MODE != 1); the writer stores the
-// update (MODE != 1) and its Courant/hydro candidates (MODE != 0).
+// The writer's part of phase 2: the element's update from the results o of
+// its repetitions (MODE != 1) and its Courant/hydro candidates (MODE != 0).
 template <int MODE>
-__device__ __forceinline__ void material_update(const DevState &s, const MatItem &m,
-                                                double &dtc, double &dth)
+__device__ __forceinline__ void material_finish(const DevState &s, const MatItem &m,
+                                                const EosOut &o, double &dtc, double &dth)
 {
     const Params &P = s.prm;
     const int ielem = m.ielem;
     if (MODE != 1) {
-        double p_new, e_new, q_new, ss_new;
-        eval_eos(P, m.e, m.delv, m.p, m.q_old, m.qquad, m.qlin, m.vnewc, m.reps, p_new, e_new,
-                 q_new, ss_new, m.writer);
-        if (m.writer) {
-            s.qq[ielem] = m.qquad;
-            s.ql[ielem] = m.qlin;
-            s.p[ielem] = p_new;
-            s.e[ielem] = e_new;
-            s.q[ielem] = q_new;
-            s.ss[ielem] = ss_new;
+        s.qq[ielem] = m.qquad;
+        s.ql[ielem] = m.qlin;
+        s.p[ielem] = o.p;
+        s.e[ielem] = o.e;
+        s.q[ielem] = o.q;
+        s.ss[ielem] = eos_sound_speed(P, o, m.vnewc);
 
-            // UpdateVolumesForElems, lulesh.cc:2410-2427
-            double tmpV = m.vnew;
-            if (dabs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
-            s.v[ielem] = tmpV;
-        }
+        // UpdateVolumesForElems, lulesh.cc:2410-2427
+        double tmpV = m.vnew;
+        if (dabs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
+        s.v[ielem] = tmpV;
     }
-    if (MODE != 0 && m.writer) {
+    if (MODE != 0) {
         // CalcCourantConstraintForElems (2447-2513) and
         // CalcHydroConstraintForElems (2517-2572) for one element.  The
         // reference evaluates the Courant dt of every element but keeps it
@@ -483,6 +489,72 @@ __device__ __forceinline__ void material_update(const DevState &s, const MatItem
     }
 }
 
+// Phase 2: the item's EOS repetitions (MODE != 1); the writer finishes the
+// element.
+template <int MODE>
+__device__ __forceinline__ void material_update(const DevState &s, const MatItem &m,
+                                                double &dtc, double &dth)
+{
+    EosOut o{};
+    if (MODE != 1)
+        o = eos_reps(s.prm, m.e, m.delv, m.p, m.q_old, m.qquad, m.qlin, m.vnewc, m.reps);
+    if (m.writer) material_finish<MODE>(s, m, o, dtc, dth);
+}
+
+// k_material on a mesh whose costly elements are shared by several items
+// (nItems != E), in three phases over the block's items and the distinct
+// elements they belong to (slots; DevState::slotElem / itemSlot):
+//   1. one thread per element: limiter, qstop check, clamps -> shared memory
+//   2. one thread per item: its share of the EOS repetitions; the writer
+//      puts the results in shared memory
+//   3. one thread per element: sound speed, stores, volume update, dt
+//      candidates
+// Phases 1 and 3 run once per element, in as few warps as the block has
+// elements, instead of once per item in warps where only the writers are
+// live.  Each element's arithmetic is that of material_load/update.
+template <int MODE, int BS>
+__device__ __forceinline__ void material_phased(const DevState &s, double &dtc, double &dth)
+{
+    __shared__ double sh_in[7][BS];
+    __shared__ double sh_out[5][BS];
+    const int g = blockIdx.x * BS + threadIdx.x;
+    const int j = threadIdx.x;
+    MatItem m;
+    m.ielem = s.slotElem[g];
+    m.writer = true;
+    if (MODE != 1 && m.ielem >= 0) {
+        material_inputs(s, m.ielem, s.ctl, m);
+        sh_in[0][j] = m.e;
+        sh_in[1][j] = m.delv;
+        sh_in[2][j] = m.p;
+        sh_in[3][j] = m.q_old;
+        sh_in[4][j] = m.qquad;
+        sh_in[5][j] = m.qlin;
+        sh_in[6][j] = m.vnewc;
+    }
+    EosOut o{};
+    if (MODE != 1) {
+        __syncthreads();
+        const int slot = g < s.nItems ? s.itemSlot[g] : -1;
+        if (slot >= 0) {
+            const int r = s.regRep[g];
+            const EosOut w = eos_reps(s.prm, sh_in[0][slot], sh_in[1][slot], sh_in[2][slot],
+                                      sh_in[3][slot], sh_in[4][slot], sh_in[5][slot],
+                                      sh_in[6][slot], r > 0 ? r : -r);
+            if (r > 0) {
+                sh_out[0][slot] = w.p;
+                sh_out[1][slot] = w.e;
+                sh_out[2][slot] = w.q;
+                sh_out[3][slot] = w.bvc;
+                sh_out[4][slot] = w.pbvc;
+            }
+        }
+        __syncthreads();
+        if (m.ielem >= 0) o = {sh_out[0][j], sh_out[1][j], sh_out[2][j], sh_out[3][j], sh_out[4][j]};
+    }
+    if (m.ielem >= 0) material_finish<MODE>(s, m, o, dtc, dth);
+}
+
 // MODE 0: Q limiter + qstop + EOS + sound speed + volume update (the part of
 //         LagrangeElements after the kinematics)
 // MODE 1: time constraints only (CalcTimeConstraintsForElems)
@@ -495,14 +567,12 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
     if (!BATCHED && !cycle_live(s.ctl)) return;
     double dtc = 1.0e+20, dth = 1.0e+20;
     if (!BATCHED) {
+        // one item per element (nItems == E); meshes with shared elements
+        // run k_material_shared
         const int t = blockIdx.x * BS + threadIdx.x;
         MatItem m;
-        const bool have = t < s.nItems && material_load<MODE>(s, t, s.ctl, m);
-        // An element's items share this block: every item has read the
-        // element's state before its writer stores the update.  Without
-        // shared elements (nItems == E) no item waits for another.
-        if (s.nItems != s.E) __syncthreads();
-        if (have) material_update<MODE>(s, m, dtc, dth);
+        if (t < s.nItems && material_load<MODE>(s, t, s.ctl, m))
+            material_update<MODE>(s, m, dtc, dth);
         if (MODE != 0)
             finish_dt<BS>(s, dtc, dth, MODE == 2);
         else
@@ -524,6 +594,20 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
         batched_dt_candidates(s, pid, dtc, dth);
     }
     finish_batched(s);
+}
+
+// k_material on a mesh whose costly elements are shared by several work
+// items (nItems != E; material_phased), single problem only.
+template <int MODE, int BS>
+__global__ void __launch_bounds__(BS) k_material_shared(DevState s)
+{
+    if (!cycle_live(s.ctl)) return;
+    double dtc = 1.0e+20, dth = 1.0e+20;
+    material_phased<MODE, BS>(s, dtc, dth);
+    if (MODE != 0)
+        finish_dt<BS>(s, dtc, dth, MODE == 2);
+    else
+        finish_material_flags(s);
 }
 
 }  // namespace LG_NS

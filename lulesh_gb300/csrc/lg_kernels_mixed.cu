@@ -2,7 +2,8 @@
 //
 // FP32, on element-relative coordinates (node positions minus node 0's,
 // differenced in FP64 and then converted): stress and hourglass forces, the
-// per-corner force scratch and its per-node sums, the characteristic length,
+// per-corner force scratch (one summed stress + hourglass force per corner
+// and component) and its per-node sums, the characteristic length,
 // the velocity gradient and the monotonic-Q gradients and limiter.
 // FP64: node coordinates and velocities and their update, the element volume
 // and relative volume (CalcElemVolume differences nearly equal coordinates),
@@ -53,22 +54,30 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
     for (int j = 0; j < 8; ++j) nd[j] = __ldg(&s.nodelistT[(size_t)j * E + k]);
     float x[8], y[8], z[8];
     relative_coords(s, nd, x, y, z);
+    // stress corner forces, kept until the hourglass forces are added: one
+    // summed force per corner and component goes to the scratch
+    float fs[3][8];
     {
         const float sig = to_f32(-s.p[k] - s.q[k]);
         const float determ = jacobian_det(x, y, z);
-        float pfx[8], pfy[8], pfz[8];
-        node_normals(pfx, pfy, pfz, x, y, z);
+        node_normals(fs[0], fs[1], fs[2], x, y, z);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            cs[0 * E8 + (size_t)j * E + k] = -(sig * pfx[j]);
-            cs[1 * E8 + (size_t)j * E + k] = -(sig * pfy[j]);
-            cs[2 * E8 + (size_t)j * E + k] = -(sig * pfz[j]);
+            fs[0][j] = -(sig * fs[0][j]);
+            fs[1][j] = -(sig * fs[1][j]);
+            fs[2][j] = -(sig * fs[2][j]);
         }
         if (determ <= 0.f) raise_status(ctl, -1);
     }
     const double vk = s.v[k];
     if (vk <= 0.0) raise_status(ctl, -1);
-    if (!(hg64 > 0.)) return;
+    if (!(hg64 > 0.)) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) cs[c * E8 + (size_t)j * E + k] = fs[c][j];
+        return;
+    }
     const float determ = to_f32(s.volo[k]) * to_f32(vk);
     float hourgam[8][4];
     {
@@ -108,9 +117,9 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
         }
 #pragma unroll
         for (int i = 0; i < 8; i++)
-            cs[(3 + c) * E8 + (size_t)i * E + k] =
-                coefficient * (hourgam[i][0] * hxx[0] + hourgam[i][1] * hxx[1] +
-                               hourgam[i][2] * hxx[2] + hourgam[i][3] * hxx[3]);
+            cs[c * E8 + (size_t)i * E + k] =
+                fs[c][i] + coefficient * (hourgam[i][0] * hxx[0] + hourgam[i][1] * hxx[1] +
+                                          hourgam[i][2] * hxx[2] + hourgam[i][3] * hxx[3]);
     }
 }
 
@@ -126,32 +135,21 @@ __global__ void __launch_bounds__(BS) k_forces(DevState s)
     }
 }
 
-// ordered FP32 corner gather, then LagrangeNodal's FP64 node update
-// (lulesh.cc:1139-1219)
-__device__ __forceinline__ void nodes_node(const DevState &s, const int n, const Ctl *ctl,
-                                           const bool hg)
+// ordered FP32 gather of the corners' summed stress + hourglass forces,
+// then LagrangeNodal's FP64 node update (lulesh.cc:1139-1219)
+__device__ __forceinline__ void nodes_node(const DevState &s, const int n, const Ctl *ctl)
 {
     const int E = s.E;
     const size_t E8 = 8 * (size_t)E;
     const float *cs = fview(s.corner);
     const int b = s.nodeElemStart[n], e = s.nodeElemStart[n + 1];
-    float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
     for (int i = b; i < e; ++i) {
         const int c = s.nodeElemCornerList[i];
         const size_t idx = (size_t)(c & 7) * E + (c >> 3);
         fx += cs[0 * E8 + idx];
         fy += cs[1 * E8 + idx];
         fz += cs[2 * E8 + idx];
-        if (hg) {
-            hx += cs[3 * E8 + idx];
-            hy += cs[4 * E8 + idx];
-            hz += cs[5 * E8 + idx];
-        }
-    }
-    if (hg) {
-        fx += hx;
-        fy += hy;
-        fz += hz;
     }
     const double Fx = to_f64(fx), Fy = to_f64(fy), Fz = to_f64(fz);
     s.fx[n] = Fx;
@@ -190,7 +188,7 @@ __global__ void __launch_bounds__(BS) k_nodes(DevState s)
         const int pid = BATCHED ? s.nodeProb[n] : 0;
         const Ctl *ctl = s.ctl + pid;
         if (BATCHED && !cycle_live(ctl)) continue;
-        nodes_node(s, n, ctl, (BATCHED ? s.hgcoefs[pid] : s.prm.hgcoef) > 0.);
+        nodes_node(s, n, ctl);
     }
 }
 
@@ -413,113 +411,99 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
     }
 }
 
-// One work item of k_material, as in the FP64 kernels (MatItem there):
-// regRep > 0 the element's writer, < 0 a share of its EOS repetitions,
-// regPerm < 0 padding.
+// An element of k_material's shared-item path (material_phased): its
+// limiter results, clamped volumes and EOS inputs (MatItem of the FP64
+// kernels; reps and writer are unused here).
 struct MatItem {
     int ielem, reps;
     bool writer;
     double qlin, qquad, q_old, vnewc, vnew, e, delv, p;
 };
 
-// Phase 1, reads only: Q limiter (FP32), qstop check and material clamps
-// (MODE != 1).  False for padding.
-template <int MODE>
-__device__ __forceinline__ bool material_load(const DevState &s, const int t, Ctl *ctl,
-                                              MatItem &m)
+// The element part of phase 1, reads only: Q limiter (FP32), qstop check and
+// material clamps of element ielem.
+__device__ __forceinline__ void material_inputs(const DevState &s, const int ielem, Ctl *ctl,
+                                                MatItem &m)
 {
     const Params &P = s.prm;
-    const int ielem = s.regPerm[t];
-    if (ielem < 0) return false;
-    const int r = s.regRep[t];
-    m.ielem = ielem;
-    m.writer = r > 0;
-    m.reps = r > 0 ? r : -r;
-    if (MODE != 1) {
-        const float lm = to_f32(P.monoq_limiter_mult), ms = to_f32(P.monoq_max_slope);
-        const float *gvx = fview(s.delv_xi), *gve = fview(s.delv_eta),
-                    *gvz = fview(s.delv_zeta);
-        const int bc = s.elemBC[ielem];
-        const float phixi = monoq_phi(lm, ms, gvx, ielem, bc, XI_M_SYMM, XI_M_FREE, XI_M,
-                                      XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
-                                      s.lxip[ielem]);
-        const float phieta = monoq_phi(lm, ms, gve, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
-                                       ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P, s.letam[ielem],
-                                       s.letap[ielem]);
-        const float phizeta = monoq_phi(lm, ms, gvz, ielem, bc, ZETA_M_SYMM, ZETA_M_FREE,
-                                        ZETA_M, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P,
-                                        s.lzetam[ielem], s.lzetap[ielem]);
-        const double vnew = s.vnew[ielem];
-        const double vdov = s.vdov[ielem];
-        double qlin, qquad;
-        if (FastOps::lt(0.0, vdov)) {
-            qlin = 0.;
-            qquad = 0.;
-        } else {
-            float dxxi = gvx[ielem] * fview(s.delx_xi)[ielem];
-            float dxeta = gve[ielem] * fview(s.delx_eta)[ielem];
-            float dxzeta = gvz[ielem] * fview(s.delx_zeta)[ielem];
-            if (dxxi > 0.f) dxxi = 0.f;
-            if (dxeta > 0.f) dxeta = 0.f;
-            if (dxzeta > 0.f) dxzeta = 0.f;
-            const float rho = to_f32(s.elemMass[ielem]) /
-                              (to_f32(s.volo[ielem]) * to_f32(vnew));
-            qlin = to_f64(-to_f32(P.qlc_monoq) * rho *
-                          (dxxi * (1.f - phixi) + dxeta * (1.f - phieta) +
-                           dxzeta * (1.f - phizeta)));
-            qquad = to_f64(to_f32(P.qqc_monoq) * rho *
-                           (dxxi * dxxi * (1.f - phixi * phixi) +
-                            dxeta * dxeta * (1.f - phieta * phieta) +
-                            dxzeta * dxzeta * (1.f - phizeta * phizeta)));
-        }
-        m.qlin = qlin;
-        m.qquad = qquad;
-
-        m.q_old = s.q[ielem];
-        if (FastOps::lt(P.qstop, m.q_old)) ctl->err_qstop = 1;
-
-        double vnewc = vnew;
-        if (P.eosvmin != 0. && FastOps::lt(vnewc, P.eosvmin)) vnewc = P.eosvmin;
-        if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vnewc)) vnewc = P.eosvmax;
-        double vc = s.v[ielem];
-        if (P.eosvmin != 0. && FastOps::lt(vc, P.eosvmin)) vc = P.eosvmin;
-        if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vc)) vc = P.eosvmax;
-        if (FastOps::le(vc, 0.)) ctl->err_matvol = 1;
-        m.vnewc = vnewc;
-        m.vnew = vnew;
-        m.e = s.e[ielem];
-        m.delv = s.delv[ielem];
-        m.p = s.p[ielem];
+    const float lm = to_f32(P.monoq_limiter_mult), ms = to_f32(P.monoq_max_slope);
+    const float *gvx = fview(s.delv_xi), *gve = fview(s.delv_eta),
+                *gvz = fview(s.delv_zeta);
+    const int bc = s.elemBC[ielem];
+    const float phixi = monoq_phi(lm, ms, gvx, ielem, bc, XI_M_SYMM, XI_M_FREE, XI_M,
+                                  XI_P_SYMM, XI_P_FREE, XI_P, s.lxim[ielem],
+                                  s.lxip[ielem]);
+    const float phieta = monoq_phi(lm, ms, gve, ielem, bc, ETA_M_SYMM, ETA_M_FREE,
+                                   ETA_M, ETA_P_SYMM, ETA_P_FREE, ETA_P, s.letam[ielem],
+                                   s.letap[ielem]);
+    const float phizeta = monoq_phi(lm, ms, gvz, ielem, bc, ZETA_M_SYMM, ZETA_M_FREE,
+                                    ZETA_M, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P,
+                                    s.lzetam[ielem], s.lzetap[ielem]);
+    const double vnew = s.vnew[ielem];
+    const double vdov = s.vdov[ielem];
+    double qlin, qquad;
+    if (FastOps::lt(0.0, vdov)) {
+        qlin = 0.;
+        qquad = 0.;
+    } else {
+        float dxxi = gvx[ielem] * fview(s.delx_xi)[ielem];
+        float dxeta = gve[ielem] * fview(s.delx_eta)[ielem];
+        float dxzeta = gvz[ielem] * fview(s.delx_zeta)[ielem];
+        if (dxxi > 0.f) dxxi = 0.f;
+        if (dxeta > 0.f) dxeta = 0.f;
+        if (dxzeta > 0.f) dxzeta = 0.f;
+        const float rho = to_f32(s.elemMass[ielem]) /
+                          (to_f32(s.volo[ielem]) * to_f32(vnew));
+        qlin = to_f64(-to_f32(P.qlc_monoq) * rho *
+                      (dxxi * (1.f - phixi) + dxeta * (1.f - phieta) +
+                       dxzeta * (1.f - phizeta)));
+        qquad = to_f64(to_f32(P.qqc_monoq) * rho *
+                       (dxxi * dxxi * (1.f - phixi * phixi) +
+                        dxeta * dxeta * (1.f - phieta * phieta) +
+                        dxzeta * dxzeta * (1.f - phizeta * phizeta)));
     }
-    return true;
+    m.qlin = qlin;
+    m.qquad = qquad;
+
+    m.q_old = s.q[ielem];
+    if (FastOps::lt(P.qstop, m.q_old)) ctl->err_qstop = 1;
+
+    double vnewc = vnew;
+    if (P.eosvmin != 0. && FastOps::lt(vnewc, P.eosvmin)) vnewc = P.eosvmin;
+    if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vnewc)) vnewc = P.eosvmax;
+    double vc = s.v[ielem];
+    if (P.eosvmin != 0. && FastOps::lt(vc, P.eosvmin)) vc = P.eosvmin;
+    if (P.eosvmax != 0. && FastOps::lt(P.eosvmax, vc)) vc = P.eosvmax;
+    if (FastOps::le(vc, 0.)) ctl->err_matvol = 1;
+    m.vnewc = vnewc;
+    m.vnew = vnew;
+    m.e = s.e[ielem];
+    m.delv = s.delv[ielem];
+    m.p = s.p[ielem];
 }
 
-// Phase 2: the item's FP64 EOS repetitions (MODE != 1); the writer stores
-// the update (MODE != 1) and its FP64 Courant/hydro candidates (MODE != 0).
+// The writer's part of phase 2: the element's update from the results o of
+// its FP64 repetitions (MODE != 1) and its FP64 Courant/hydro candidates
+// (MODE != 0).
 template <int MODE>
-__device__ __forceinline__ void material_update(const DevState &s, const MatItem &m,
-                                                double &dtc, double &dth)
+__device__ __forceinline__ void material_finish(const DevState &s, const MatItem &m,
+                                                const EosOut &o, double &dtc, double &dth)
 {
     const Params &P = s.prm;
     const int ielem = m.ielem;
     if (MODE != 1) {
-        double p_new, e_new, q_new, ss_new;
-        eval_eos<FastOps>(P, m.e, m.delv, m.p, m.q_old, m.qquad, m.qlin, m.vnewc, m.reps,
-                          p_new, e_new, q_new, ss_new, m.writer);
-        if (m.writer) {
-            s.qq[ielem] = m.qquad;
-            s.ql[ielem] = m.qlin;
-            s.p[ielem] = p_new;
-            s.e[ielem] = e_new;
-            s.q[ielem] = q_new;
-            s.ss[ielem] = ss_new;
+        s.qq[ielem] = m.qquad;
+        s.ql[ielem] = m.qlin;
+        s.p[ielem] = o.p;
+        s.e[ielem] = o.e;
+        s.q[ielem] = o.q;
+        s.ss[ielem] = eos_sound_speed<FastOps>(P, o, m.vnewc);
 
-            double tmpV = m.vnew;
-            if (FastOps::abs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
-            s.v[ielem] = tmpV;
-        }
+        double tmpV = m.vnew;
+        if (FastOps::abs_lt(tmpV - 1.0, P.v_cut)) tmpV = 1.0;
+        s.v[ielem] = tmpV;
     }
-    if (MODE != 0 && m.writer) {
+    if (MODE != 0) {
         // Only elements with vdov != 0 constrain dt; a warp of elements at
         // rest skips the FP64 square root and reciprocals altogether.
         const double vdov = s.vdov[ielem];
@@ -538,23 +522,62 @@ __device__ __forceinline__ void material_update(const DevState &s, const MatItem
     }
 }
 
+// k_material when costly elements are shared by several items, in three
+// phases as in the FP64 kernels (material_phased there): per element the
+// inputs, per item the repetitions, per element the finish.
+template <int MODE, int BS>
+__device__ __forceinline__ void material_phased(const DevState &s, double &dtc, double &dth)
+{
+    __shared__ double sh_in[7][BS];
+    __shared__ double sh_out[5][BS];
+    const int g = blockIdx.x * BS + threadIdx.x;
+    const int j = threadIdx.x;
+    MatItem m;
+    m.ielem = s.slotElem[g];
+    m.writer = true;
+    if (MODE != 1 && m.ielem >= 0) {
+        material_inputs(s, m.ielem, s.ctl, m);
+        sh_in[0][j] = m.e;
+        sh_in[1][j] = m.delv;
+        sh_in[2][j] = m.p;
+        sh_in[3][j] = m.q_old;
+        sh_in[4][j] = m.qquad;
+        sh_in[5][j] = m.qlin;
+        sh_in[6][j] = m.vnewc;
+    }
+    EosOut o{};
+    if (MODE != 1) {
+        __syncthreads();
+        const int slot = g < s.nItems ? s.itemSlot[g] : -1;
+        if (slot >= 0) {
+            const int r = s.regRep[g];
+            const EosOut w = eos_reps<FastOps>(s.prm, sh_in[0][slot], sh_in[1][slot],
+                                               sh_in[2][slot], sh_in[3][slot], sh_in[4][slot],
+                                               sh_in[5][slot], sh_in[6][slot], r > 0 ? r : -r);
+            if (r > 0) {
+                sh_out[0][slot] = w.p;
+                sh_out[1][slot] = w.e;
+                sh_out[2][slot] = w.q;
+                sh_out[3][slot] = w.bvc;
+                sh_out[4][slot] = w.pbvc;
+            }
+        }
+        __syncthreads();
+        if (m.ielem >= 0) o = {sh_out[0][j], sh_out[1][j], sh_out[2][j], sh_out[3][j], sh_out[4][j]};
+    }
+    if (m.ielem >= 0) material_finish<MODE>(s, m, o, dtc, dth);
+}
+
 template <int MODE, bool BATCHED, int BS>
 __global__ void __launch_bounds__(BS) k_material(DevState s)
 {
     if (!BATCHED && !cycle_live(s.ctl)) return;
     double dtc = 1.0e+20, dth = 1.0e+20;
     if (!BATCHED) {
+        // one item per element (nItems == E); meshes with shared elements
+        // run k_material_shared
         const int t = blockIdx.x * BS + threadIdx.x;
-        if (s.nItems == s.E) {
-            if (t < s.E) material_element<MODE>(s, t, s.ctl, dtc, dth);
-        } else {
-            MatItem m;
-            const bool have = t < s.nItems && material_load<MODE>(s, t, s.ctl, m);
-            // An element's items share this block: every item has read the
-            // element's state before its writer stores the update.
-            __syncthreads();
-            if (have) material_update<MODE>(s, m, dtc, dth);
-        }
+        if (t < s.E) material_element<MODE>(s, t, s.ctl, dtc, dth);
         if (MODE != 0)
             finish_dt<BS>(s, dtc, dth, MODE == 2);
         else
@@ -574,6 +597,20 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
         batched_dt_candidates(s, pid, dtc, dth);
     }
     finish_batched(s);
+}
+
+// k_material on a mesh whose costly elements are shared by several work
+// items (nItems != E; material_phased), single problem only.
+template <int MODE, int BS>
+__global__ void __launch_bounds__(BS) k_material_shared(DevState s)
+{
+    if (!cycle_live(s.ctl)) return;
+    double dtc = 1.0e+20, dth = 1.0e+20;
+    material_phased<MODE, BS>(s, dtc, dth);
+    if (MODE != 0)
+        finish_dt<BS>(s, dtc, dth, MODE == 2);
+    else
+        finish_material_flags(s);
 }
 
 }  // namespace mixed

@@ -127,6 +127,26 @@ int build_work_items(const Problem &p, long long resident, int block,
     return writers;
 }
 
+void build_item_slots(const std::vector<int> &item_elem, int block, std::vector<int> &slot_elem,
+                      std::vector<int> &item_slot)
+{
+    const size_t n = item_elem.size();
+    const size_t blocks = (n + block - 1) / block;
+    slot_elem.assign(blocks * block, -1);
+    item_slot.assign(n, -1);
+    for (size_t b = 0; b < blocks; ++b) {
+        int slots = 0, prev = -1;
+        for (size_t t = b * block; t < std::min(n, (b + 1) * block); ++t) {
+            const int e = item_elem[t];
+            if (e < 0) continue;
+            // an element's items are consecutive and never straddle a block
+            if (e != prev) slot_elem[b * block + slots++] = e;
+            item_slot[t] = slots - 1;
+            prev = e;
+        }
+    }
+}
+
 void build_corner_list(Problem &p)
 {
     const int N = p.numNode, E = p.numElem;

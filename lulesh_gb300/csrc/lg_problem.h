@@ -111,6 +111,14 @@ std::vector<int> region_visit_order(int numReg, int cost);
 int build_work_items(const Problem &p, long long resident, int block,
                      std::vector<int> &item_elem, std::vector<int> &item_rep);
 
+// Slots of the material kernel's shared-item path: for block b of `block`
+// items, slot_elem[b*block + j] is the j-th distinct element among its items
+// (in order of first appearance; -1 past the last), and item_slot[t] the
+// slot of item t's element within its block (-1 for padding).  slot_elem
+// covers ceil(items / block) whole blocks.
+void build_item_slots(const std::vector<int> &item_elem, int block, std::vector<int> &slot_elem,
+                      std::vector<int> &item_slot);
+
 // End-of-run report text, lulesh-util.cc:175-230.
 std::string format_report(int nx, int cycle, double e0, double maxAbsDiff,
                           double totalAbsDiff, double maxRelDiff, double elapsed);

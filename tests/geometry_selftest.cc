@@ -90,6 +90,57 @@ int main(int argc, char **argv)
         check("char_length", geo_ref_char_length(x, y, z, vol), char_length(x, y, z, vol));
     }
 
+    // the FP32 sign filter of the Jacobian determinant: it may only claim
+    // "positive" where the FP64 determinant is positive.  Elements: unit
+    // cubes at offsets up to 1e3 with sizes from 1e-6 to 10 (large offsets
+    // against small sizes push the coordinate rounding), jittered, flattened
+    // toward a plane, collapsed toward a node, and inverted (two nodes
+    // swapped).
+    long certain = 0, shaped = 0, claimed_wrong = 0;
+    std::uniform_real_distribution<double> lsz(-6.0, 1.0), loff(-3.0, 3.0);
+    for (long it = 0; it < 4 * n; ++it) {
+        const double h = std::pow(10.0, lsz(g)), off = std::pow(10.0, loff(g));
+        const int kind = (int)(it % 5);
+        const double o[3] = {off * u(g), off * u(g), off * u(g)};
+        double x[8], y[8], z[8];
+        for (int j = 0; j < 8; ++j) {
+            const double jit = kind == 1 ? 0.3 : 0.0;
+            x[j] = o[0] + h * (cx[j] + jit * u(g));
+            y[j] = o[1] + h * (cy[j] + jit * u(g));
+            z[j] = o[2] + h * (cz[j] + jit * u(g));
+            if (kind == 2) z[j] = o[2] + h * std::pow(10.0, -8.0 * std::fabs(u(g))) * cz[j];
+        }
+        if (kind == 3) {  // node 6 collapsed onto node 0, nearly
+            const double t = std::pow(10.0, -10.0 * std::fabs(u(g)));
+            x[6] = x[0] + t * (x[6] - x[0]);
+            y[6] = y[0] + t * (y[6] - y[0]);
+            z[6] = z[0] + t * (z[6] - z[0]);
+        }
+        if (kind == 4) {  // inverted: nodes 0 and 6 swapped
+            std::swap(x[0], x[6]);
+            std::swap(y[0], y[6]);
+            std::swap(z[0], z[6]);
+        }
+        const bool sure = jacobian_certainly_positive(x, y, z);
+        const double det = jacobian_det(x, y, z);
+        if (sure && !(det > 0.0)) {
+            if (claimed_wrong < 10)
+                std::printf("filter claimed a positive determinant: %.17g (kind %d)\n", det, kind);
+            ++claimed_wrong;
+        }
+        if (kind == 0 && off < 1e3 * h) {  // coordinates up to 1e3 element sizes, as s <= 1000
+            ++shaped;
+            certain += sure;
+        }
+    }
+    g_bad += claimed_wrong;
+    std::printf("jacobian filter: %ld wrong claims; certain for %ld of %ld cubes\n", claimed_wrong,
+                certain, shaped);
+    if (certain < shaped) {
+        std::printf("filter undecided on a well-shaped cube\n");
+        ++g_bad;
+    }
+
     // monotonic-Q gradients: the oracle's domain-level loop on a jittered
     // mesh with random velocities and relative volumes
     orc_domain *d = orc_create(6, 11, 1, 1);

@@ -202,3 +202,24 @@ def test_large_problem_few_cycles(lg, oracle_built, precision):
     o.step(3)
     for f in ("x", "xd", "e", "p", "q", "v", "ss"):
         assert field_rel_err(d.field(f), o.field(f)) <= FP64_TOL, f
+
+
+@pytest.mark.parametrize("precision", BUILDS + ["mixed"])
+def test_region_change_after_capture(lg, precision):
+    """Replacing regNumList re-plans the material kernel's work items (their
+    count, and with it the kernel variant).  A handle whose cycle graphs were
+    already captured must then run exactly as one that got the new regions
+    before its first cycle."""
+    a = lg.Domain(12, 11, 1, 1, precision=precision)
+    assert a.step(3) == 0              # captures the cycle graphs
+    a.reset()
+    reg = a.field("regNumList").copy()
+    reg[:] = 11                        # every element in the costliest region
+    reg[::7] = 1
+    a.set_field("regNumList", reg)
+    assert a.step(20) == 0
+    b = lg.Domain(12, 11, 1, 1, precision=precision)
+    b.set_field("regNumList", reg)
+    assert b.step(20) == 0
+    for k in _fields():
+        assert np.array_equal(a.field(k).view(np.int64), b.field(k).view(np.int64)), k

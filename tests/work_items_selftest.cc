@@ -3,7 +3,9 @@
 // every element has exactly one writer item, the shares of its items add up
 // to its region's EOS repetition count, an element's items never straddle a
 // block of 128, the count stays within what the handle reserves
-// (numElem + 2 x resident), and a mesh whose repeated counts all reach
+// (numElem + 2 x resident), the slots of the shared-item path
+// (lg::build_item_slots) list each block's distinct elements once with every
+// item pointing at its element's slot, and a mesh whose repeated counts all reach
 // T = 3/8 resident keeps one item per element in the plain region order.  Prints one line per case
 // and the number of failed checks; exits 1 if any.
 #include <cstdio>
@@ -60,6 +62,37 @@ int main()
                   "shares add up to the region's repetitions", nx);
         }
         for (const auto &b : blocks) check(b.second.size() == 1, "items within one block", nx);
+        // slots of the shared-item path: per block its distinct elements in
+        // order, every item pointing at its own element's slot
+        std::vector<int> slot_elem, item_slot;
+        lg::build_item_slots(item_elem, 128, slot_elem, item_slot);
+        check(slot_elem.size() == (item_elem.size() + 127) / 128 * 128, "slot array covers blocks",
+              nx);
+        check(item_slot.size() == item_elem.size(), "one slot per item", nx);
+        std::vector<int> slotted(p.numElem, 0);
+        for (size_t b = 0; b * 128 < item_elem.size(); ++b) {
+            bool ended = false;
+            for (int j = 0; j < 128; ++j) {
+                const int e = slot_elem[b * 128 + j];
+                if (e < 0) {
+                    ended = true;
+                    continue;
+                }
+                check(!ended, "slots are dense", nx);
+                check(e < p.numElem, "slot element in range", nx);
+                slotted[e]++;
+            }
+        }
+        for (int e = 0; e < p.numElem; ++e) check(slotted[e] == 1, "each element in one slot", nx);
+        for (size_t i = 0; i < item_elem.size(); ++i) {
+            if (item_elem[i] < 0) {
+                check(item_slot[i] == -1, "padding has no slot", nx);
+                continue;
+            }
+            check(item_slot[i] >= 0 && item_slot[i] < 128 &&
+                      slot_elem[(i / 128) * 128 + item_slot[i]] == item_elem[i],
+                  "item slot names its element", nx);
+        }
         // a mesh where every repeated count has at least T elements keeps one
         // item per element, in plain region order
         std::map<int, long long> count;
