@@ -599,20 +599,30 @@ def run_gpu(a):
     d.reset()
     for f in fields:
         d.field(f, out=host[f])
+    init = {f: host[f].copy() for f in fields}
     h2d = sum(host[f].nbytes for f in fields)
-    _barrier(dist)
-    t0 = time.perf_counter()
-    for f in fields:
-        d.set_field(f, host[f])
-    st2 = d.step(a.steps)
-    for f in fields:
-        d.field(f, out=host[f])
-    t_e2e = time.perf_counter() - t0
-    _barrier(dist)
-    t_e2e = _max_over_ranks(dist, t_e2e)
+    # host <-> device copies of a short window vary from run to run (the
+    # download of the 26 fields took 4 to 40 ms in repeated runs at s=150):
+    # the median of three end-to-end runs, each from the initial state
+    reps = 3 if a.steps <= 100 else 1
+    times, st2 = [], 0
+    for _ in range(reps):
+        d.reset()  # the time-step state back to cycle 0 (untimed)
+        for f in fields:
+            host[f][:] = init[f]
+        _barrier(dist)
+        t0 = time.perf_counter()
+        for f in fields:
+            d.set_field(f, host[f])
+        st2 = d.step(a.steps) or st2
+        for f in fields:
+            d.field(f, out=host[f])
+        times.append(time.perf_counter() - t0)
+        _barrier(dist)
+    t_e2e = _max_over_ranks(dist, statistics.median(times))
     e2e = {"value": ws * E * a.steps / (t_e2e * 1e6), "unit": UNIT,
            "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": h2d / a.steps,
-           "status": st2}
+           "status": st2, "runs": reps, "run_seconds": times}
 
     # the same when the caller keeps the reference's Domain on the host and
     # syncs it around every cycle (the second binding of the integration

@@ -94,6 +94,7 @@ cudaError_t device_setup(const DevState &s, int nx, double einit, bool topology,
                          int pid = 0);
 cudaError_t device_verify(const double *e, int nx, double *scratch, double *out,
                           cudaStream_t stream);
+cudaError_t device_inv_mass(const double *m, double *inv, long long n, cudaStream_t stream);
 }  // namespace lg
 
 namespace {
@@ -134,44 +135,42 @@ int upload(lg_domain *d, T *dst, const std::vector<T> &src)
     return LG_OK;
 }
 
-// 1 / nodalMass for the mixed path's acceleration, from the host values m
-int upload_inv_mass(lg_domain *d, const double *m, size_t n)
+// invMass = RN(1 / nodalMass) from the masses on the device (the nodal
+// accelerations of every path)
+int refresh_inv_mass(lg_domain *d)
 {
-    std::vector<double> inv(n);
-    for (size_t i = 0; i < n; ++i) inv[i] = 1.0 / m[i];
-    return upload(d, d->ds.invMass, inv);
+    LG_CUDA(lg::device_inv_mass(d->ds.nodalMass, d->ds.invMass, d->ds.N, d->stream));
+    return LG_OK;
 }
 
-// regNumList and k_material's work items (DevState::nItems), built on the
-// host by lg::build_work_items: elements in region order, the regions with
-// the most EOS repetitions first, each region's elements in their ascending
-// regElemlist order.  On a small mesh the costly regions fill too few blocks
-// to keep every SM's FP64 pipe busy (at s=30 the 8,445 elements with 20
-// repetitions make 66 blocks for 152 SMs), so their elements get several
-// items that share the repetitions.  All items of an element sit in one
-// block of 128, and the kernel's barrier orders every item's reads before
-// the writer's stores: the work done and the results are unchanged.
+// regNumList and the material phase's work items (DevState::nItems), built
+// on the host by lg::build_material_items.  Large meshes: one item per
+// element in region order, the regions with the most EOS repetitions first,
+// each region's elements in their ascending regElemlist order.  Small
+// meshes, where the costly regions would fill too few blocks to keep every
+// SM's FP64 pipe busy (at s=30 the 8,445 elements with 20 repetitions make 66
+// blocks for 152 SMs), run the phase split (DevState::matSplit): repetition
+// items of equal shares carry the EOS work, and the per-element parts run
+// once per element.  The work done and the results are the same either way.
 int upload_regions(lg_domain *d)
 {
     const lg::Problem &p = d->prob;
     std::vector<int> perm, rep;
-    if (lg::build_work_items(p, d->resident, 128, perm, rep) != p.numElem)
+    const bool split = lg::build_material_items(p, d->resident, perm, rep);
+    if (!split && (int)perm.size() != p.numElem)
         return set_error(LG_ERR_INVALID, "region sets do not cover all elements");
     if ((long long)perm.size() > d->item_cap)
         return set_error(LG_ERR_STATE, "%zu work items exceed the capacity %d", perm.size(),
                          d->item_cap);
-    std::vector<int> slot_elem, item_slot;
-    lg::build_item_slots(perm, 128, slot_elem, item_slot);
     int st;
     if ((st = upload(d, d->ds.regNumList, p.regNumList))) return st;
     if ((st = upload(d, d->ds.regPerm, perm))) return st;
     if ((st = upload(d, d->ds.regRep, rep))) return st;
-    if ((st = upload(d, d->ds.slotElem, slot_elem))) return st;
-    if ((st = upload(d, d->ds.itemSlot, item_slot))) return st;
-    // the graphs hold the kernel arguments (nItems) and the material kernel
+    // the graphs hold the kernel arguments (nItems) and the material kernels
     // chosen for them
-    if (d->ds.nItems != (int)perm.size()) drop_graphs(d);
+    if (d->ds.nItems != (int)perm.size() || d->ds.matSplit != (int)split) drop_graphs(d);
     d->ds.nItems = (int)perm.size();
+    d->ds.matSplit = split ? 1 : 0;
     LG_CUDA(cudaStreamSynchronize(d->stream));
     return LG_OK;
 }
@@ -321,6 +320,9 @@ int write_ctl(lg_domain *d)
     return LG_OK;
 }
 
+// kernels one cycle launches: four, or six when the material phase runs split
+int kernels_per_cycle(const lg_domain *d) { return d->ds.matSplit ? 6 : 4; }
+
 void enqueue_cycle(lg_domain *d)
 {
     d->ks->launch(lg::K_FORCES, d->ds, 0, d->stream);
@@ -370,7 +372,7 @@ int enqueue_cycles(lg_domain *d, int ncycles)
     }
     while (left-- > 0) LG_CUDA(cudaGraphLaunch(d->graph1, d->stream));
     LG_CUDA(cudaGetLastError());
-    d->launches += 1 + 4LL * ncycles;
+    d->launches += 1 + (long long)kernels_per_cycle(d) * ncycles;
     return LG_OK;
 }
 
@@ -396,7 +398,7 @@ int upload_initial_state(lg_domain *d, bool creating)
             find_f64(d, names[i], &fld, &cnt);
             if ((st = upload(d, fld, *hostf[i]))) return st;
         }
-        if ((st = upload_inv_mass(d, p.nodalMass.data(), p.nodalMass.size()))) return st;
+        if ((st = refresh_inv_mass(d))) return st;
     } else {
         LG_CUDA(lg::device_setup(d->ds, p.nx, lg::sedov_einit(p.nx, d->opts.einit_factor),
                                  creating && !d->mirror_topo, d->stream));
@@ -529,9 +531,9 @@ int lg_create(const lg_opts *opts, lg_domain **out)
         sms < 1)
         sms = 1;
     d->resident = sms * 8 * 128;  // 8 blocks of 128 threads per SM (64 registers)
-    // upload_regions adds at most T = 3/8 resident items for each of the two
-    // split repetition counts, plus padding of at most 31 in 128
-    d->item_cap = (int)(E + 2 * (size_t)d->resident);
+    // split material phase: at most E + 4 x resident repetition items (each
+    // element's count rounded up, the total bounded by 4 x resident shares)
+    d->item_cap = (int)(E + 4 * (size_t)d->resident);
     const int eblocks = (int)((d->item_cap + 127) / 128);
 
     Layout L;
@@ -543,8 +545,7 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     size_t o_conn[7];
     for (auto &o : o_conn) o = L.add<int>(E);
     const size_t o_regnum = L.add<int>(E), o_perm = L.add<int>(d->item_cap),
-                 o_rep = L.add<int>(d->item_cap), o_slot = L.add<int>((size_t)eblocks * 128),
-                 o_islot = L.add<int>(d->item_cap);
+                 o_rep = L.add<int>(d->item_cap);
     const size_t o_nes = L.add<int>(N + 1), o_ncl = L.add<int>(8 * E);
     const size_t o_symm = L.add<uint8_t>(N);
     const size_t o_part = L.add<double>(2 * (size_t)eblocks);
@@ -578,8 +579,6 @@ int lg_create(const lg_opts *opts, lg_domain **out)
     s.regNumList = reinterpret_cast<int *>(base + o_regnum);
     s.regPerm = reinterpret_cast<int *>(base + o_perm);
     s.regRep = reinterpret_cast<int *>(base + o_rep);
-    s.slotElem = reinterpret_cast<int *>(base + o_slot);
-    s.itemSlot = reinterpret_cast<int *>(base + o_islot);
     s.nodeElemStart = reinterpret_cast<int *>(base + o_nes);
     s.nodeElemCornerList = reinterpret_cast<int *>(base + o_ncl);
     s.symm = reinterpret_cast<uint8_t *>(base + o_symm);
@@ -670,7 +669,7 @@ int lg_step_timed(lg_domain *d, int ncycles, double *ms)
     }
     while (left-- > 0) LG_CUDA(cudaGraphLaunch(d->graph1, d->stream));
     LG_CUDA(cudaEventRecord(d->ev1, d->stream));
-    d->launches += 1 + 4LL * ncycles;
+    d->launches += 1 + (long long)kernels_per_cycle(d) * ncycles;
     LG_CUDA(cudaEventSynchronize(d->ev1));
     float f = 0.f;
     LG_CUDA(cudaEventElapsedTime(&f, d->ev0, d->ev1));
@@ -788,9 +787,7 @@ int lg_set_field(lg_domain *d, const char *name, const void *src, size_t n)
     if (find_f64(d, name, &p, &c)) {
         if (n != c) return set_error(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, c, n);
         LG_CUDA(cudaMemcpyAsync(p, src, c * sizeof(double), cudaMemcpyHostToDevice, d->stream));
-        if (!strcmp(name, "nodalMass") &&
-            (st = upload_inv_mass(d, static_cast<const double *>(src), c)))
-            return st;
+        if (!strcmp(name, "nodalMass") && (st = refresh_inv_mass(d))) return st;
         LG_CUDA(cudaStreamSynchronize(d->stream));
         return LG_OK;
     }

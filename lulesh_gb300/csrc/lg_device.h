@@ -72,14 +72,17 @@ struct DevState {
     double *e, *p, *q, *ql, *qq, *v, *volo, *vnew, *delv, *vdov, *arealg, *ss, *elemMass;
     double *delx_xi, *delx_eta, *delx_zeta, *delv_xi, *delv_eta, *delv_zeta;
     int *regNumList, *regPerm, *regRep;
-    // work items of k_material: regPerm / regRep hold nItems entries (one per
-    // element, or on small meshes several per element of the costly regions,
-    // each with a share of the EOS repetitions; the element's last one is its
-    // writer, regRep > 0; padding has regPerm < 0).  Ensembles: nItems = E.
+    // work items of the material phase: regPerm / regRep hold nItems entries
+    // (one per element in region order, regRep its repetitions; or, when the
+    // phase runs split, repetition items: an element and a share of its EOS
+    // repetitions, regRep > 0 for its writer and < 0 for the others).
+    // Ensembles: nItems = E.
     int nItems;
-    // the shared-item path's slots (lg::build_item_slots): per block of 128
-    // items its distinct elements, and per item its element's slot
-    int *slotElem, *itemSlot;
+    // 1: the material phase runs split (small meshes; lg::build_material_items):
+    // k_material_inputs over the elements, k_material_eos over the nItems
+    // repetition items, k_material_finish over the elements, staging the
+    // EOS inputs and results in the per-corner scratch (free in that phase)
+    int matSplit;
     // block sizes of the single-problem element kernels (k_forces,
     // k_kinematics) and of k_nodes: 32, 64 or 128 (0 means 128), chosen at
     // creation so that small meshes spread evenly over the SMs

@@ -27,6 +27,7 @@ namespace lg {
 int record_error(int code, const char *msg);
 cudaError_t device_setup(const DevState &s, int nx, double einit, bool topology,
                          cudaStream_t stream, int eoff, int noff, long long tstride, int pid);
+cudaError_t device_inv_mass(const double *m, double *inv, long long n, cudaStream_t stream);
 }
 
 namespace {
@@ -576,13 +577,9 @@ int lg_ensemble_set_field(lg_ensemble *en, int prob, const char *name, const voi
     if (n != cnt) return err(LG_ERR_INVALID, "field '%s' has %zu entries, not %zu", name, cnt, n);
     double *dst = dev_f64(en->ds, name) + (node ? en->noff[prob] : en->eoff[prob]);
     EN_CUDA(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, en->stream));
-    if (!strcmp(name, "nodalMass")) {
-        const double *m = static_cast<const double *>(src);
-        std::vector<double> inv(cnt);
-        for (size_t i = 0; i < cnt; ++i) inv[i] = 1.0 / m[i];
-        EN_CUDA(cudaMemcpyAsync(en->ds.invMass + en->noff[prob], inv.data(), cnt * sizeof(double),
-                                cudaMemcpyHostToDevice, en->stream));
-    }
+    if (!strcmp(name, "nodalMass"))  // RN(1 / m) of the member's masses, on the device
+        EN_CUDA(lg::device_inv_mass(dst, en->ds.invMass + en->noff[prob], (long long)cnt,
+                                    en->stream));
     EN_CUDA(cudaStreamSynchronize(en->stream));
     return LG_OK;
 }

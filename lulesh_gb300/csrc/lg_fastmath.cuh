@@ -19,28 +19,23 @@
 namespace lg {
 namespace fast {
 
-// double -> float, rounded to nearest (ties to even), on the integer pipe:
-// the magnitude's bits re-biased from the double to the float exponent, then
-// rounded on their 29 dropped bits by one 64-bit add (half an ulp less one,
-// plus the kept mantissa's lowest bit, which turns exact ties to even); a
-// carry out of the mantissa steps the exponent, and from the largest finite
-// float to infinity.  Values below the float normal range become zero,
-// values above it infinity.
+// double -> float, rounded to nearest (ties to even), on the integer pipe in
+// 32-bit operations: the high word re-biased from the double to the float
+// exponent and joined with the top 3 bits of the low word gives the
+// truncated float; its 29 dropped bits plus its lowest kept bit plus half an
+// ulp less one carry into bit 29 exactly when the value rounds up (ties to
+// even), and that carry steps the mantissa, the exponent on overflow, and
+// the largest finite float to infinity.  Values below the float normal range
+// become zero, values above it infinity.
 __device__ __forceinline__ float to_f32(double v)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-    // exponent - 1023 + 127 <= 0 (the magnitude's top bits below 897 << 52)
-    const long long t = (long long)((b & 0x7fffffffffffffffull) - (896ull << 52));
-    unsigned r;
-    if (t < (1ll << 52)) {
-        r = 0u;
-    } else {
-        const unsigned long long q =
-            ((unsigned long long)t + 0x0fffffffull + (((unsigned long long)t >> 29) & 1ull)) >> 29;
-        r = q >= 0x7f800000ull ? 0x7f800000u : (unsigned)q;
-    }
-    return __uint_as_float(sign | r);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned mag = hi & 0x7fffffffu, ed = mag >> 20;
+    unsigned r = ((mag - (896u << 20)) << 3) | (lo >> 29);
+    r += ((lo & 0x1fffffffu) + (r & 1u) + 0x0fffffffu) >> 29;
+    r = ed <= 896u ? 0u : (ed >= 1151u ? 0x7f800000u : r);
+    return __uint_as_float((hi & 0x80000000u) | r);
 }
 
 // float -> double, exact for normal values (float subnormals become zero).

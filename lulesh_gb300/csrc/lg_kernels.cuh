@@ -12,13 +12,13 @@
 //   k_kinematics  per element: volume, vnew, delv, arealg, vdov
 //                 (CalcKinematicsForElems) and the monotonic-Q gradients
 //                 (CalcMonotonicQGradientsForElems)
-//   k_material    per work item in region order (an element, or on small
-//                 meshes a share of an element's EOS repetitions):
-//                 monotonic-Q limiter, qstop check, EOS with its
-//                 repetitions, sound speed, volume update, Courant/hydro
-//                 constraints with a block reduction; its last block
-//                 finishes the reduction and runs the next cycle's
-//                 TimeIncrement
+//   k_material    per element in region order: monotonic-Q limiter, qstop
+//                 check, EOS with its repetitions, sound speed, volume
+//                 update, Courant/hydro constraints with a block reduction;
+//                 its last block finishes the reduction and runs the next
+//                 cycle's TimeIncrement.  Small meshes run the same work as
+//                 k_material_inputs (per element), k_material_eos (per
+//                 repetition item) and k_material_finish (per element)
 //
 // Every arithmetic expression keeps the reference's operand order (see the
 // oracle's lulesh_oracle.c for the line-by-line correspondence), with two
@@ -356,13 +356,12 @@ __global__ void __launch_bounds__(BS) k_kinematics(DevState s)
     }
 }
 
-// One work item of k_material: an element at region-order position t with
-// all its EOS repetitions, or on small meshes a share of them (see
-// upload_regions in lg_api.cu).  regRep[t] > 0 marks the element's writer,
-// which stores the update and the Courant/hydro candidates; < 0 marks a
-// share whose results are dropped; regPerm[t] < 0 is padding.  Every
-// repetition computes the same values from the same inputs, so the writer's
-// are the update.
+// One element of the material phase: its id and EOS repetitions (work item
+// t of k_material, region order: regPerm[t], regRep[t]; every such item is
+// its element's writer), its limiter results, clamped volumes and EOS
+// inputs.  Every repetition computes the same values from the same inputs,
+// so any repetition's results are the update; the split kernels for small
+// meshes rely on that too.
 struct MatItem {
     int ielem, reps;
     bool writer;
@@ -431,7 +430,7 @@ __device__ __forceinline__ void material_inputs(const DevState &s, const int iel
 }
 
 // Phase 1 of item t: its element, repetitions and role, and (MODE != 1) the
-// element's inputs.  False for padding.
+// element's inputs.  False for an item without an element.
 template <int MODE>
 __device__ __forceinline__ bool material_load(const DevState &s, const int t, Ctl *ctl,
                                               MatItem &m)
@@ -501,74 +500,103 @@ __device__ __forceinline__ void material_update(const DevState &s, const MatItem
     if (m.writer) material_finish<MODE>(s, m, o, dtc, dth);
 }
 
-// k_material on a mesh whose costly elements are shared by several items
-// (nItems != E), in three phases over the block's items and the distinct
-// elements they belong to (slots; DevState::slotElem / itemSlot):
-//   1. one thread per element: limiter, qstop check, clamps -> shared memory
-//   2. one thread per item: its share of the EOS repetitions; the writer
-//      puts the results in shared memory
-//   3. one thread per element: sound speed, stores, volume update, dt
-//      candidates
-// Phases 1 and 3 run once per element, in as few warps as the block has
-// elements, instead of once per item in warps where only the writers are
-// live.  Each element's arithmetic is that of material_load/update.
+// The split material phase (DevState::matSplit, small meshes): three
+// kernels instead of one, so that every FP64 instruction runs with full
+// warps.  k_material_inputs (one thread per element, natural order): the
+// monotonic-Q limiter, qstop check and clamps, staging the EOS inputs;
+// k_material_eos (one thread per repetition item, equal shares per warp):
+// the item's share of the EOS repetitions, the writer staging the results;
+// k_material_finish (one thread per element): sound speed, stores, volume
+// update, Courant/hydro candidates and the block reduction whose last block
+// runs the next TimeIncrement.  The staging area is the per-corner scratch,
+// which k_nodes has consumed and the next k_forces overwrites: eight inputs
+// and five results per element, SoA.  Each element's arithmetic is that of
+// the one-kernel path.
+namespace matstage {
+enum { E_OLD, DELV, P_OLD, Q_OLD, QQ, QL, VNEWC, VNEW, N_IN };
+enum { P_NEW = N_IN, E_NEW, Q_NEW, BVC, PBVC, N_ALL };
+}  // namespace matstage
+
 template <int MODE, int BS>
-__device__ __forceinline__ void material_phased(const DevState &s, double &dtc, double &dth)
+__global__ void __launch_bounds__(BS) k_material_inputs(DevState s)
 {
-    __shared__ double sh_in[7][BS];
-    __shared__ double sh_out[5][BS];
-    const int g = blockIdx.x * BS + threadIdx.x;
-    const int j = threadIdx.x;
+    if (!cycle_live(s.ctl)) return;
+    const int k = blockIdx.x * BS + threadIdx.x;
+    if (k >= s.E) return;
     MatItem m;
-    m.ielem = s.slotElem[g];
-    m.writer = true;
-    if (MODE != 1 && m.ielem >= 0) {
-        material_inputs(s, m.ielem, s.ctl, m);
-        sh_in[0][j] = m.e;
-        sh_in[1][j] = m.delv;
-        sh_in[2][j] = m.p;
-        sh_in[3][j] = m.q_old;
-        sh_in[4][j] = m.qquad;
-        sh_in[5][j] = m.qlin;
-        sh_in[6][j] = m.vnewc;
-    }
-    EosOut o{};
-    if (MODE != 1) {
-        __syncthreads();
-        const int slot = g < s.nItems ? s.itemSlot[g] : -1;
-        if (slot >= 0) {
-            const int r = s.regRep[g];
-            const EosOut w = eos_reps(s.prm, sh_in[0][slot], sh_in[1][slot], sh_in[2][slot],
-                                      sh_in[3][slot], sh_in[4][slot], sh_in[5][slot],
-                                      sh_in[6][slot], r > 0 ? r : -r);
-            if (r > 0) {
-                sh_out[0][slot] = w.p;
-                sh_out[1][slot] = w.e;
-                sh_out[2][slot] = w.q;
-                sh_out[3][slot] = w.bvc;
-                sh_out[4][slot] = w.pbvc;
-            }
-        }
-        __syncthreads();
-        if (m.ielem >= 0) o = {sh_out[0][j], sh_out[1][j], sh_out[2][j], sh_out[3][j], sh_out[4][j]};
-    }
-    if (m.ielem >= 0) material_finish<MODE>(s, m, o, dtc, dth);
+    material_inputs(s, k, s.ctl, m);
+    double *st = s.corner;
+    const size_t E = (size_t)s.E;
+    st[matstage::E_OLD * E + k] = m.e;
+    st[matstage::DELV * E + k] = m.delv;
+    st[matstage::P_OLD * E + k] = m.p;
+    st[matstage::Q_OLD * E + k] = m.q_old;
+    st[matstage::QQ * E + k] = m.qquad;
+    st[matstage::QL * E + k] = m.qlin;
+    st[matstage::VNEWC * E + k] = m.vnewc;
+    st[matstage::VNEW * E + k] = m.vnew;
 }
 
-// MODE 0: Q limiter + qstop + EOS + sound speed + volume update (the part of
-//         LagrangeElements after the kinematics)
-// MODE 1: time constraints only (CalcTimeConstraintsForElems)
-// MODE 2: both, then the next cycle's TimeIncrement (the fused main loop)
-// BATCHED (MODE 2 only): positions of many problems; each problem's minima go
-// to its slots, and the last block finishes every live problem's cycle.
+template <int BS>
+__global__ void __launch_bounds__(BS) k_material_eos(DevState s)
+{
+    if (!cycle_live(s.ctl)) return;
+    const int t = blockIdx.x * BS + threadIdx.x;
+    if (t >= s.nItems) return;
+    const int k = s.regPerm[t], r = s.regRep[t];
+    double *st = s.corner;
+    const size_t E = (size_t)s.E;
+    const EosOut o = eos_reps(s.prm, st[matstage::E_OLD * E + k], st[matstage::DELV * E + k],
+                              st[matstage::P_OLD * E + k], st[matstage::Q_OLD * E + k],
+                              st[matstage::QQ * E + k], st[matstage::QL * E + k],
+                              st[matstage::VNEWC * E + k], r > 0 ? r : -r);
+    if (r > 0) {
+        st[matstage::P_NEW * E + k] = o.p;
+        st[matstage::E_NEW * E + k] = o.e;
+        st[matstage::Q_NEW * E + k] = o.q;
+        st[matstage::BVC * E + k] = o.bvc;
+        st[matstage::PBVC * E + k] = o.pbvc;
+    }
+}
+
+template <int MODE, int BS>
+__global__ void __launch_bounds__(BS) k_material_finish(DevState s)
+{
+    if (!cycle_live(s.ctl)) return;
+    double dtc = 1.0e+20, dth = 1.0e+20;
+    const int k = blockIdx.x * BS + threadIdx.x;
+    if (k < s.E) {
+        MatItem m;
+        m.ielem = k;
+        m.writer = true;
+        EosOut o{};
+        if (MODE != 1) {
+            const double *st = s.corner;
+            const size_t E = (size_t)s.E;
+            m.qquad = st[matstage::QQ * E + k];
+            m.qlin = st[matstage::QL * E + k];
+            m.vnewc = st[matstage::VNEWC * E + k];
+            m.vnew = st[matstage::VNEW * E + k];
+            o = {st[matstage::P_NEW * E + k], st[matstage::E_NEW * E + k],
+                 st[matstage::Q_NEW * E + k], st[matstage::BVC * E + k],
+                 st[matstage::PBVC * E + k]};
+        }
+        material_finish<MODE>(s, m, o, dtc, dth);
+    }
+    if (MODE != 0)
+        finish_dt<BS>(s, dtc, dth, MODE == 2);
+    else
+        finish_material_flags(s);
+}
+
 template <int MODE, bool BATCHED, int BS>
 __global__ void __launch_bounds__(BS) k_material(DevState s)
 {
     if (!BATCHED && !cycle_live(s.ctl)) return;
     double dtc = 1.0e+20, dth = 1.0e+20;
     if (!BATCHED) {
-        // one item per element (nItems == E); meshes with shared elements
-        // run k_material_shared
+        // one item per element (nItems == E); small meshes run the split
+        // kernels above
         const int t = blockIdx.x * BS + threadIdx.x;
         MatItem m;
         if (t < s.nItems && material_load<MODE>(s, t, s.ctl, m))
@@ -594,20 +622,6 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
         batched_dt_candidates(s, pid, dtc, dth);
     }
     finish_batched(s);
-}
-
-// k_material on a mesh whose costly elements are shared by several work
-// items (nItems != E; material_phased), single problem only.
-template <int MODE, int BS>
-__global__ void __launch_bounds__(BS) k_material_shared(DevState s)
-{
-    if (!cycle_live(s.ctl)) return;
-    double dtc = 1.0e+20, dth = 1.0e+20;
-    material_phased<MODE, BS>(s, dtc, dth);
-    if (MODE != 0)
-        finish_dt<BS>(s, dtc, dth, MODE == 2);
-    else
-        finish_material_flags(s);
 }
 
 }  // namespace LG_NS

@@ -411,7 +411,7 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
     }
 }
 
-// An element of k_material's shared-item path (material_phased): its
+// An element of the split material phase (k_material_inputs / _finish): its
 // limiter results, clamped volumes and EOS inputs (MatItem of the FP64
 // kernels; reps and writer are unused here).
 struct MatItem {
@@ -522,50 +522,93 @@ __device__ __forceinline__ void material_finish(const DevState &s, const MatItem
     }
 }
 
-// k_material when costly elements are shared by several items, in three
-// phases as in the FP64 kernels (material_phased there): per element the
-// inputs, per item the repetitions, per element the finish.
+// The split material phase (DevState::matSplit, small meshes): three
+// kernels instead of one, so that every FP64 instruction runs with full
+// warps.  k_material_inputs (one thread per element, natural order): the
+// monotonic-Q limiter, qstop check and clamps, staging the EOS inputs;
+// k_material_eos (one thread per repetition item, equal shares per warp):
+// the item's share of the EOS repetitions, the writer staging the results;
+// k_material_finish (one thread per element): sound speed, stores, volume
+// update, Courant/hydro candidates and the block reduction whose last block
+// runs the next TimeIncrement.  The staging area is the per-corner scratch,
+// which k_nodes has consumed and the next k_forces overwrites: eight inputs
+// and five results per element, SoA.  Each element's arithmetic is that of
+// the one-kernel path.
+namespace matstage {
+enum { E_OLD, DELV, P_OLD, Q_OLD, QQ, QL, VNEWC, VNEW, N_IN };
+enum { P_NEW = N_IN, E_NEW, Q_NEW, BVC, PBVC, N_ALL };
+}  // namespace matstage
+
 template <int MODE, int BS>
-__device__ __forceinline__ void material_phased(const DevState &s, double &dtc, double &dth)
+__global__ void __launch_bounds__(BS) k_material_inputs(DevState s)
 {
-    __shared__ double sh_in[7][BS];
-    __shared__ double sh_out[5][BS];
-    const int g = blockIdx.x * BS + threadIdx.x;
-    const int j = threadIdx.x;
+    if (!cycle_live(s.ctl)) return;
+    const int k = blockIdx.x * BS + threadIdx.x;
+    if (k >= s.E) return;
     MatItem m;
-    m.ielem = s.slotElem[g];
-    m.writer = true;
-    if (MODE != 1 && m.ielem >= 0) {
-        material_inputs(s, m.ielem, s.ctl, m);
-        sh_in[0][j] = m.e;
-        sh_in[1][j] = m.delv;
-        sh_in[2][j] = m.p;
-        sh_in[3][j] = m.q_old;
-        sh_in[4][j] = m.qquad;
-        sh_in[5][j] = m.qlin;
-        sh_in[6][j] = m.vnewc;
+    material_inputs(s, k, s.ctl, m);
+    double *st = s.corner;
+    const size_t E = (size_t)s.E;
+    st[matstage::E_OLD * E + k] = m.e;
+    st[matstage::DELV * E + k] = m.delv;
+    st[matstage::P_OLD * E + k] = m.p;
+    st[matstage::Q_OLD * E + k] = m.q_old;
+    st[matstage::QQ * E + k] = m.qquad;
+    st[matstage::QL * E + k] = m.qlin;
+    st[matstage::VNEWC * E + k] = m.vnewc;
+    st[matstage::VNEW * E + k] = m.vnew;
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_material_eos(DevState s)
+{
+    if (!cycle_live(s.ctl)) return;
+    const int t = blockIdx.x * BS + threadIdx.x;
+    if (t >= s.nItems) return;
+    const int k = s.regPerm[t], r = s.regRep[t];
+    double *st = s.corner;
+    const size_t E = (size_t)s.E;
+    const EosOut o = eos_reps<FastOps>(s.prm, st[matstage::E_OLD * E + k], st[matstage::DELV * E + k],
+                              st[matstage::P_OLD * E + k], st[matstage::Q_OLD * E + k],
+                              st[matstage::QQ * E + k], st[matstage::QL * E + k],
+                              st[matstage::VNEWC * E + k], r > 0 ? r : -r);
+    if (r > 0) {
+        st[matstage::P_NEW * E + k] = o.p;
+        st[matstage::E_NEW * E + k] = o.e;
+        st[matstage::Q_NEW * E + k] = o.q;
+        st[matstage::BVC * E + k] = o.bvc;
+        st[matstage::PBVC * E + k] = o.pbvc;
     }
-    EosOut o{};
-    if (MODE != 1) {
-        __syncthreads();
-        const int slot = g < s.nItems ? s.itemSlot[g] : -1;
-        if (slot >= 0) {
-            const int r = s.regRep[g];
-            const EosOut w = eos_reps<FastOps>(s.prm, sh_in[0][slot], sh_in[1][slot],
-                                               sh_in[2][slot], sh_in[3][slot], sh_in[4][slot],
-                                               sh_in[5][slot], sh_in[6][slot], r > 0 ? r : -r);
-            if (r > 0) {
-                sh_out[0][slot] = w.p;
-                sh_out[1][slot] = w.e;
-                sh_out[2][slot] = w.q;
-                sh_out[3][slot] = w.bvc;
-                sh_out[4][slot] = w.pbvc;
-            }
+}
+
+template <int MODE, int BS>
+__global__ void __launch_bounds__(BS) k_material_finish(DevState s)
+{
+    if (!cycle_live(s.ctl)) return;
+    double dtc = 1.0e+20, dth = 1.0e+20;
+    const int k = blockIdx.x * BS + threadIdx.x;
+    if (k < s.E) {
+        MatItem m;
+        m.ielem = k;
+        m.writer = true;
+        EosOut o{};
+        if (MODE != 1) {
+            const double *st = s.corner;
+            const size_t E = (size_t)s.E;
+            m.qquad = st[matstage::QQ * E + k];
+            m.qlin = st[matstage::QL * E + k];
+            m.vnewc = st[matstage::VNEWC * E + k];
+            m.vnew = st[matstage::VNEW * E + k];
+            o = {st[matstage::P_NEW * E + k], st[matstage::E_NEW * E + k],
+                 st[matstage::Q_NEW * E + k], st[matstage::BVC * E + k],
+                 st[matstage::PBVC * E + k]};
         }
-        __syncthreads();
-        if (m.ielem >= 0) o = {sh_out[0][j], sh_out[1][j], sh_out[2][j], sh_out[3][j], sh_out[4][j]};
+        material_finish<MODE>(s, m, o, dtc, dth);
     }
-    if (m.ielem >= 0) material_finish<MODE>(s, m, o, dtc, dth);
+    if (MODE != 0)
+        finish_dt<BS>(s, dtc, dth, MODE == 2);
+    else
+        finish_material_flags(s);
 }
 
 template <int MODE, bool BATCHED, int BS>
@@ -574,8 +617,8 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
     if (!BATCHED && !cycle_live(s.ctl)) return;
     double dtc = 1.0e+20, dth = 1.0e+20;
     if (!BATCHED) {
-        // one item per element (nItems == E); meshes with shared elements
-        // run k_material_shared
+        // one item per element (nItems == E); small meshes run the split
+        // kernels above
         const int t = blockIdx.x * BS + threadIdx.x;
         if (t < s.E) material_element<MODE>(s, t, s.ctl, dtc, dth);
         if (MODE != 0)
@@ -597,20 +640,6 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
         batched_dt_candidates(s, pid, dtc, dth);
     }
     finish_batched(s);
-}
-
-// k_material on a mesh whose costly elements are shared by several work
-// items (nItems != E; material_phased), single problem only.
-template <int MODE, int BS>
-__global__ void __launch_bounds__(BS) k_material_shared(DevState s)
-{
-    if (!cycle_live(s.ctl)) return;
-    double dtc = 1.0e+20, dth = 1.0e+20;
-    material_phased<MODE, BS>(s, dtc, dth);
-    if (MODE != 0)
-        finish_dt<BS>(s, dtc, dth, MODE == 2);
-    else
-        finish_material_flags(s);
 }
 
 }  // namespace mixed

@@ -89,62 +89,63 @@ std::vector<int> region_visit_order(int numReg, int cost)
     return order;
 }
 
-int build_work_items(const Problem &p, long long resident, int block,
-                     std::vector<int> &item_elem, std::vector<int> &item_rep)
+bool build_material_items(const Problem &p, long long resident, std::vector<int> &item_elem,
+                          std::vector<int> &item_rep)
 {
     // elements per repetition count
     std::map<int, long long> count;
     for (int r = 0; r < p.numReg; ++r)
         count[region_rep(r, p.numReg, p.cost)] += (long long)p.regElemlist[r].size();
     const long long T = 3 * resident / 8;
-    auto items_of = [&](int rr) -> int {
-        const long long n = count[rr];
-        if (rr < 2 || n >= T || n == 0) return 1;
-        return (int)std::min<long long>({(T + n - 1) / n, (long long)rr, 32LL});
-    };
+    bool split = false;
+    for (const auto &kv : count)
+        if (kv.first >= 2 && kv.second > 0 && kv.second < T) split = true;
     item_elem.clear();
     item_rep.clear();
-    item_elem.reserve(p.numElem);
-    item_rep.reserve(p.numElem);
-    int writers = 0;
-    for (const int r : region_visit_order(p.numReg, p.cost)) {
-        const int rr = region_rep(r, p.numReg, p.cost);
-        const int f = items_of(rr);
-        for (int e : p.regElemlist[r]) {
-            if (f > 1 && (int)(item_elem.size() % block) + f > block)
-                while (item_elem.size() % block) {
-                    item_elem.push_back(-1);
-                    item_rep.push_back(0);
-                }
-            for (int i = 0; i < f; ++i) {
-                const int share = rr / f + (i < rr % f ? 1 : 0);
+    if (!split) {
+        // one item per element, in region visit order (each region's
+        // elements in their ascending regElemlist order)
+        item_elem.reserve(p.numElem);
+        item_rep.reserve(p.numElem);
+        for (const int r : region_visit_order(p.numReg, p.cost)) {
+            const int rr = region_rep(r, p.numReg, p.cost);
+            for (int e : p.regElemlist[r]) {
                 item_elem.push_back(e);
-                item_rep.push_back(i == f - 1 ? share : -share);
+                item_rep.push_back(rr);
             }
-            ++writers;
         }
+        return false;
     }
-    return writers;
-}
-
-void build_item_slots(const std::vector<int> &item_elem, int block, std::vector<int> &slot_elem,
-                      std::vector<int> &item_slot)
-{
-    const size_t n = item_elem.size();
-    const size_t blocks = (n + block - 1) / block;
-    slot_elem.assign(blocks * block, -1);
-    item_slot.assign(n, -1);
-    for (size_t b = 0; b < blocks; ++b) {
-        int slots = 0, prev = -1;
-        for (size_t t = b * block; t < std::min(n, (b + 1) * block); ++t) {
-            const int e = item_elem[t];
-            if (e < 0) continue;
-            // an element's items are consecutive and never straddle a block
-            if (e != prev) slot_elem[b * block + slots++] = e;
-            item_slot[t] = slots - 1;
-            prev = e;
-        }
+    // repetition items of at most R repetitions: the element's repetitions
+    // in near-equal shares, its first item the writer; R keeps the count
+    // near 4 x resident or below
+    long long total = 0;
+    for (const auto &kv : count) total += (long long)kv.first * kv.second;
+    const long long R = std::max<long long>(1, (total + 4 * resident - 1) / (4 * resident));
+    std::vector<int> region_of(p.numElem, 0);
+    for (int r = 0; r < p.numReg; ++r)
+        for (int e : p.regElemlist[r]) region_of[e] = r;
+    struct Item {
+        int elem, share;
+        bool writer;
+    };
+    std::vector<Item> items;
+    for (int e = 0; e < p.numElem; ++e) {
+        const int rr = region_rep(region_of[e], p.numReg, p.cost);
+        const int n = (int)((rr + R - 1) / R);
+        for (int i = 0; i < n; ++i)
+            items.push_back({e, rr / n + (i < rr % n ? 1 : 0), i == 0});
     }
+    // the largest shares first, so that a warp's items carry equal shares
+    std::stable_sort(items.begin(), items.end(),
+                     [](const Item &a, const Item &b) { return a.share > b.share; });
+    item_elem.reserve(items.size());
+    item_rep.reserve(items.size());
+    for (const Item &it : items) {
+        item_elem.push_back(it.elem);
+        item_rep.push_back(it.writer ? it.share : -it.share);
+    }
+    return true;
 }
 
 void build_corner_list(Problem &p)

@@ -98,26 +98,17 @@ int region_rep(int r, int numReg, int cost);
 // the grid keeps them from forming a tail that leaves SMs idle.
 std::vector<int> region_visit_order(int numReg, int cost);
 
-// Work items of the material kernel (one per element, or on a small mesh
-// several per element of a costly repetition count, each with a share of the
-// element's EOS repetitions).  Fills item_elem (element id, -1 for padding)
-// and item_rep (> 0: the element's writer with that many repetitions, < 0: a
-// share of -item_rep repetitions, 0: padding), in region visit order.  A
-// repetition count whose elements number fewer than 3/8 of `resident` (the
-// threads of one resident wave) gets f = min(ceil(T / count), rep, 32) items
-// per element, T = 3/8 resident; an element's items never straddle a block
-// of `block` threads.  Returns the number of writers, which is numElem when
-// the region sets cover every element once.
-int build_work_items(const Problem &p, long long resident, int block,
-                     std::vector<int> &item_elem, std::vector<int> &item_rep);
-
-// Slots of the material kernel's shared-item path: for block b of `block`
-// items, slot_elem[b*block + j] is the j-th distinct element among its items
-// (in order of first appearance; -1 past the last), and item_slot[t] the
-// slot of item t's element within its block (-1 for padding).  slot_elem
-// covers ceil(items / block) whole blocks.
-void build_item_slots(const std::vector<int> &item_elem, int block, std::vector<int> &slot_elem,
-                      std::vector<int> &item_slot);
+// The material phase's work items.  Large meshes: one item per element
+// (item_rep = the element's EOS repetitions), in region visit order; returns
+// false.  When a repeated count's elements number fewer than T = 3/8 of
+// `resident` (the threads of one resident wave), the phase runs split
+// (k_material_inputs / k_material_eos / k_material_finish) and the items are
+// repetition items: each element's repetitions in near-equal shares of at
+// most R = max(1, ceil(total repetitions / (4 resident))), its first item
+// the writer (item_rep > 0; the others < 0), sorted by share, largest
+// first; returns true.
+bool build_material_items(const Problem &p, long long resident, std::vector<int> &item_elem,
+                          std::vector<int> &item_rep);
 
 // End-of-run report text, lulesh-util.cc:175-230.
 std::string format_report(int nx, int cycle, double e0, double maxAbsDiff,

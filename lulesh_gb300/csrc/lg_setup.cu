@@ -232,6 +232,19 @@ int blocks_for(long long n)
 
 }  // namespace
 
+__global__ void k_inv_mass(const double *m, double *inv, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) inv[i] = 1.0 / m[i];  // the IEEE quotient, as the host's
+}
+
+// Queue inv[i] = RN(1 / m[i]) for n nodal masses already on the device.
+cudaError_t device_inv_mass(const double *m, double *inv, long long n, cudaStream_t stream)
+{
+    if (n > 0) k_inv_mass<<<blocks_for(n), kSetupBlock, 0, stream>>>(m, inv, n);
+    return cudaGetLastError();
+}
+
 // Queue the self-check of the energy field e of an nx^3 mesh: out[0..3] =
 // origin energy, MaxAbsDiff, TotalAbsDiff, MaxRelDiff.  scratch holds at
 // least nx * nx doubles.

@@ -1,7 +1,7 @@
 """The mixed path's integer-pipe conversions (lg_fastmath.cuh) against the
 hardware's own: to_f32 rounds to nearest, ties to even, like
-__double2float_rn wherever the float result is normal or zero, and to_f64
-widens exactly (tests/fastmath_selftest.cu, built with nvcc and run on the
+__double2float_rn for every input that is zero or at least the smallest
+normal float, and to_f64 widens exactly (tests/fastmath_selftest.cu, built with nvcc and run on the
 GPU)."""
 import os
 import shutil

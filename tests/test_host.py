@@ -137,9 +137,11 @@ def test_ensemble_sample_is_deterministic_and_in_range(native_lib):
 
 
 def test_material_work_items(tmp_path):
-    """lg::build_work_items on the reference's region draws: one writer per
-    element, shares adding up to the region's repetitions, an element's items
-    within one block, within the reserved capacity (work_items_selftest.cc)."""
+    """lg::build_material_items on the reference's region draws: one item per
+    element in region order on large meshes; on small ones repetition items
+    with one writer per element, shares adding up to the region's repetitions
+    and sorted largest first, within the reserved capacity
+    (work_items_selftest.cc)."""
     if not shutil.which("g++"):
         pytest.skip("no host C++ compiler")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
