@@ -229,7 +229,7 @@ def cpu_reference_rate(a, budget_s: float, warmup: int, max_cycles: int) -> dict
         done += 1
     o.close()
     return {"value": E * done / (t * 1e6) if t > 0 else 0.0, "unit": UNIT, "cores": threads,
-            "kind": "port",
+            "host_nproc": os.cpu_count(), "kind": "port",
             "sample": f"{done} cycles of s={a.nx} r={a.regions} b={a.balance} c={a.cost} "
                       f"after {warmup} warm-up cycles ({t:.1f} s timed, set-up {setup:.1f} s "
                       f"untimed); oracle C restatement -O3 -fopenmp, {threads} threads"}
@@ -384,8 +384,9 @@ def cpu_ensemble_rate(members, budget_s: float) -> dict:
         ran += 1
         o.close()
     return {"value": done_ec / (t * 1e6) if t else 0.0, "unit": UNIT, "cores": threads,
-            "kind": "port", "sample": f"the first {ran} members in order, up to 300 cycles each, "
-                                      f"{t:.1f} s timed; oracle C restatement, {threads} threads"}
+            "host_nproc": os.cpu_count(), "kind": "port",
+            "sample": f"the first {ran} members in order, up to 300 cycles each, "
+                      f"{t:.1f} s timed; oracle C restatement, {threads} threads"}
 
 
 def run_reference(a):

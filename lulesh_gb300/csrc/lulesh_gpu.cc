@@ -84,10 +84,17 @@ std::vector<double> get_f64(lg_domain *d, const char *name, size_t n)
     return v;
 }
 
-// The fields of DumpDomainToVisit (lulesh-viz.cc:120-259) -- node
-// coordinates, the hexahedra, the region of each element, e, p, v, q per
-// element and xd, yd, zd and speed per node, the last ones in single
-// precision as the reference writes them -- in a binary legacy VTK file.
+std::vector<float> get_f32(lg_domain *d, const char *name, size_t n)
+{
+    const std::vector<double> v = get_f64(d, name, n);
+    return std::vector<float>(v.begin(), v.end());
+}
+
+// The content of DumpDomainToVisit (lulesh-viz.cc:120-259) in a binary legacy
+// VTK file: the cycle and time (:159-160), node coordinates in single
+// precision (:150-165), the hexahedra (:131-146), each element's region number
+// (:171-179), e, p, v, q per element (:181-218) and speed, xd, yd, zd per node
+// (:220-252), all values in single precision as the reference writes them.
 // LULESH's corner order is VTK's hexahedron order.
 int write_vtk(lg_domain *d, const char *path)
 {
@@ -100,10 +107,10 @@ int write_vtk(lg_domain *d, const char *path)
     FILE *f = fopen(path, "wb");
     if (!f) return -1;
     fprintf(f, "# vtk DataFile Version 3.0\nLULESH cycle %d time %.9e\nBINARY\n"
-               "DATASET UNSTRUCTURED_GRID\nPOINTS %zu double\n", (int)cyc, time, N);
-    const std::vector<double> x = get_f64(d, "x", N), y = get_f64(d, "y", N),
-                              z = get_f64(d, "z", N);
-    std::vector<double> xyz(3 * N);
+               "DATASET UNSTRUCTURED_GRID\nPOINTS %zu float\n", (int)cyc, time, N);
+    const std::vector<float> x = get_f32(d, "x", N), y = get_f32(d, "y", N),
+                             z = get_f32(d, "z", N);
+    std::vector<float> xyz(3 * N);
     for (size_t i = 0; i < N; ++i) {
         xyz[3 * i] = x[i];
         xyz[3 * i + 1] = y[i];
@@ -126,18 +133,14 @@ int write_vtk(lg_domain *d, const char *path)
     lg_get_field(d, "regNumList", reg.data(), E);
     put_be(f, reg);
     for (const char *name : {"e", "p", "v", "q"}) {
-        fprintf(f, "\nSCALARS %s double 1\nLOOKUP_TABLE default\n", name);
-        put_be(f, get_f64(d, name, E));
+        fprintf(f, "\nSCALARS %s float 1\nLOOKUP_TABLE default\n", name);
+        put_be(f, get_f32(d, name, E));
     }
-    const std::vector<double> xd = get_f64(d, "xd", N), yd = get_f64(d, "yd", N),
-                              zd = get_f64(d, "zd", N);
-    std::vector<float> fx(N), fy(N), fz(N), speed(N);
-    for (size_t i = 0; i < N; ++i) {
-        fx[i] = float(xd[i]);
-        fy[i] = float(yd[i]);
-        fz[i] = float(zd[i]);
+    const std::vector<float> fx = get_f32(d, "xd", N), fy = get_f32(d, "yd", N),
+                             fz = get_f32(d, "zd", N);
+    std::vector<float> speed(N);
+    for (size_t i = 0; i < N; ++i)
         speed[i] = float(std::sqrt((fx[i] * fx[i]) + (fy[i] * fy[i]) + (fz[i] * fz[i])));
-    }
     fprintf(f, "\nPOINT_DATA %zu\n", N);
     const std::pair<const char *, const std::vector<float> *> nodal[4] = {
         {"speed", &speed}, {"xd", &fx}, {"yd", &fy}, {"zd", &fz}};

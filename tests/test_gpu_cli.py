@@ -66,8 +66,11 @@ def _read_vtk(path):
     while pos < len(data):
         s = line()
         if s.startswith("POINTS"):
-            n = int(s.split()[1])
-            out["points"] = block(3 * n, "d").reshape(n, 3)
+            n, typ = int(s.split()[1]), s.split()[2]
+            out["points_type"] = typ
+            out["points"] = block(3 * n, {"double": "d", "float": "f"}[typ]).reshape(n, 3)
+        elif s.startswith("LULESH cycle"):
+            out["cycle"], out["time"] = int(s.split()[2]), float(s.split()[4])
         elif s.startswith("CELLS "):
             n, size = map(int, s.split()[1:3])
             out["cells"] = block(size, "i").reshape(n, 9)
@@ -79,10 +82,20 @@ def _read_vtk(path):
             out["npoint"] = int(s.split()[1])
         elif s.startswith("SCALARS"):
             name, typ = s.split()[1:3]
+            out.setdefault("scalars", []).append((name, typ))
             line()  # LOOKUP_TABLE
             n = out["npoint"] if "npoint" in out else out["ncell"]
             out[name] = block(n, {"double": "d", "float": "f", "int": "i"}[typ])
     return out
+
+
+# The variables DumpDomainToVisit writes, in its order, with their types and
+# centring (lulesh-viz.cc:171-252): the region material, then DB_FLOAT zone
+# variables e, p, v, q, then DB_FLOAT node variables speed, xd, yd, zd.  Its
+# mesh coordinates are DB_FLOAT too (:150-165).
+VIZ_VARIABLES = [("regions", "int"), ("e", "float"), ("p", "float"), ("v", "float"),
+                 ("q", "float"), ("speed", "float"), ("xd", "float"), ("yd", "float"),
+                 ("zd", "float")]
 
 
 def test_cli_vtk_dump(native_lib, tmp_path):
@@ -92,17 +105,20 @@ def test_cli_vtk_dump(native_lib, tmp_path):
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout
     v = _read_vtk(path)
+    assert v["scalars"] == VIZ_VARIABLES
+    assert v["points_type"] == "float"
     d = lg.Domain(5, 11, its=20)
     assert d.run() == 0
-    assert np.array_equal(v["points"][:, 0], d.field("x"))
-    assert np.array_equal(v["points"][:, 2], d.field("z"))
+    assert v["cycle"] == 20 and v["time"] == float("%.9e" % d.scalar("time"))
+    f32 = lambda name: d.field(name).astype(np.float32)
+    for k, name in enumerate("xyz"):
+        assert np.array_equal(v["points"][:, k], f32(name)), name
     assert np.array_equal(v["cells"][:, 1:].ravel(), d.field("nodelist"))
     assert np.all(v["cells"][:, 0] == 8) and np.all(v["types"] == 12)
     assert np.array_equal(v["regions"], d.field("regNumList"))
-    for f in ("e", "p", "v", "q"):
-        assert np.array_equal(v[f], d.field(f)), f
-    xd = d.field("xd").astype(np.float32)
-    assert np.array_equal(v["xd"], xd)
-    sp = np.sqrt(xd * xd + d.field("yd").astype(np.float32) ** 2
-                 + d.field("zd").astype(np.float32) ** 2)
-    assert np.allclose(v["speed"], sp, rtol=1e-6)
+    assert v["regions"].min() >= 1 and v["regions"].max() <= 11  # region numbers from 1
+    for name in ("e", "p", "v", "q", "xd", "yd", "zd"):
+        assert np.array_equal(v[name], f32(name)), name
+    xd, yd, zd = f32("xd"), f32("yd"), f32("zd")
+    sp = np.sqrt(xd * xd + yd * yd + zd * zd)
+    assert np.allclose(v["speed"], sp, rtol=1e-6, atol=0)
