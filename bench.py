@@ -78,7 +78,7 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 FP64_SLOTS_PER_UNIT = {
     "fp64": {"k_forces": 1273, "k_nodes": 78, "k_kinematics": 700, "k_material": 860},
     "fp64-fma": {"k_forces": 785, "k_nodes": 72, "k_kinematics": 602, "k_material": 804},
-    "mixed": {"k_forces": 71, "k_nodes": 12, "k_kinematics": 120, "k_material": 607},
+    "mixed": {"k_forces": 24, "k_nodes": 12, "k_kinematics": 95, "k_material": 606},
 }
 # The workload (nx, regions, balance, cost) each build's counts were taken
 # with; k_material's depend on the region mix, the others on nothing.
@@ -92,18 +92,18 @@ FP64_LANES_PER_SM_CYCLE = 2.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit per
 # launch (elements; k_nodes: nodes): the FP64 builds from the s=150
 # captures above (the benchmark mesh itself, cycle 10; cycle 500 agrees to
-# 0.1 %), the mixed build from s=96, 16 regions, balance 2, cost 4, scaled
-# by the units a launch processes.  Well above the algorithmic bytes: the
+# 0.1 %), the mixed build from s=192, 16 regions, balance 2, cost 4 (its
+# benchmark mesh, cycle 10), scaled by the units a launch processes.  Well above the algorithmic bytes: the
 # per-corner force scratch (k_forces writes it, k_nodes reads it) and the
 # region-order gathers of k_material.
 TRAFFIC_PER_UNIT = {
     "fp64": {"k_forces": 496.0, "k_nodes": 568.3, "k_kinematics": 166.6, "k_material": 291.3},
-    "fp64-fma": {"k_forces": 496.0, "k_nodes": 567.8, "k_kinematics": 166.9, "k_material": 291.8},
-    "mixed": {"k_forces": 264.4, "k_nodes": 337.7, "k_kinematics": 120.6, "k_material": 162.6},
+    "fp64-fma": {"k_forces": 496.5, "k_nodes": 567.9, "k_kinematics": 166.6, "k_material": 291.5},
+    "mixed": {"k_forces": 219.7, "k_nodes": 277.5, "k_kinematics": 148.4, "k_material": 270.2},
 }
 TRAFFIC_SOURCE = {"fp64": "ncu DRAM bytes of the s=150 benchmark mesh (cycle 10)",
                   "fp64-fma": "ncu DRAM bytes of the s=150 benchmark mesh (cycle 10)",
-                  "mixed": "ncu DRAM bytes per unit at s=96, scaled to the mesh"}
+                  "mixed": "ncu DRAM bytes per unit at s=192 r16 b2 c4 (cycle 10), scaled to the mesh"}
 
 
 def _peaks() -> dict:
