@@ -172,18 +172,32 @@ struct IeeeOps {
     }
 };
 
+// refdens == 1 exactly (every problem the reference sets up): x / refdens
+// is then x, and the sound-speed terms skip the division.  The decision is
+// taken once, outside the repetitions: a per-term select let the compiler
+// evaluate the quotient anyway, and for elements at rest (numerator 0) that
+// quotient takes the division's long special-operand path.
+__device__ __forceinline__ bool unit_refdens(const Params &P)
+{
+    return __double_as_longlong(P.refdens) == 0x3ff0000000000000LL;
+}
+
 // sound-speed term of lulesh.cc:2083-2090, 2126-2133, 2158-2165, 2190-2197
-template <class M = IeeeOps>
+template <class M = IeeeOps, bool kUnitRho = false>
 __device__ __forceinline__ double ssc_of(double num, double rho0)
 {
-    const double ssc = (rho0 == 1.0) ? num : M::div(num, rho0);
+    const double ssc = kUnitRho ? num : M::div(num, rho0);
     // Elements at rest take the floor.  A predicated square root would still
     // occupy the FP64 pipe for a warp of them, so the sequence runs only when
-    // a converged lane of the warp needs it.
+    // a converged lane of the warp needs it.  The barrier on its operand keeps
+    // the compiler from hoisting the root above the vote, where it would run
+    // for every warp.
     const bool floor = M::le(ssc, .1111111e-36);
     double r = .3333333e-18;
     if (__any_sync(__activemask(), !floor)) {
-        const double t = M::sqrt_(floor ? 1.0 : ssc);
+        double a = floor ? 1.0 : ssc;
+        opaque(a);
+        const double t = M::sqrt_(a);
         if (!floor) r = t;
     }
     return r;
@@ -214,10 +228,10 @@ struct EosOut {
 // The rep repetitions of CalcEnergyForElems (lulesh.cc:2048-2176) with
 // CalcPressureForElems (2014-2044), as EvalEOSForElems runs them for one
 // element (2204-2324).  Every repetition is evaluated, as in the reference.
-template <class M = IeeeOps>
-__device__ __forceinline__ EosOut eos_reps(const Params &P, double e_in, double delv_in,
-                                           double p_in, double q_in, double qq_in,
-                                           double ql_in, double vnewc, int rep)
+template <class M, bool kUnitRho>
+__device__ __forceinline__ EosOut eos_reps_rho(const Params &P, double e_in, double delv_in,
+                                               double p_in, double q_in, double qq_in,
+                                               double ql_in, double vnewc, int rep)
 {
     const double rho0 = P.refdens;
     double p_new = 0., e_new = 0., q_new = 0., bvc = 0., pbvc = 0.;
@@ -245,7 +259,7 @@ __device__ __forceinline__ EosOut eos_reps(const Params &P, double e_in, double 
         if (M::lt(0., delvc)) {
             q_new = 0.;
         } else {
-            const double ssc = ssc_of<M>(pbvc * e_new + vhalf * vhalf * bvc * pHalfStep, rho0);
+            const double ssc = ssc_of<M, kUnitRho>(pbvc * e_new + vhalf * vhalf * bvc * pHalfStep, rho0);
             q_new = (ssc * ql_old + qq_old);
         }
         e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (pHalfStep + q_new));
@@ -261,7 +275,7 @@ __device__ __forceinline__ EosOut eos_reps(const Params &P, double e_in, double 
             if (M::lt(0., delvc)) {
                 q_tilde = 0.;
             } else {
-                const double ssc = ssc_of<M>(pbvc * e_new + vc * vc * bvc * p_new, rho0);
+                const double ssc = ssc_of<M, kUnitRho>(pbvc * e_new + vc * vc * bvc * p_new, rho0);
                 q_tilde = (ssc * ql_old + qq_old);
             }
             e_new = e_new - (7.0 * (p_old + q_old) - 8.0 * (pHalfStep + q_new) +
@@ -272,7 +286,7 @@ __device__ __forceinline__ EosOut eos_reps(const Params &P, double e_in, double 
 
         p_new = pressure<M>(P, bvc, pbvc, e_new, compression, vc);
         if (M::le(delvc, 0.)) {
-            const double ssc = ssc_of<M>(pbvc * e_new + vc * vc * bvc * p_new, rho0);
+            const double ssc = ssc_of<M, kUnitRho>(pbvc * e_new + vc * vc * bvc * p_new, rho0);
             q_new = (ssc * ql_old + qq_old);
             if (M::abs_lt(q_new, P.q_cut)) q_new = 0.;
         }
@@ -280,11 +294,23 @@ __device__ __forceinline__ EosOut eos_reps(const Params &P, double e_in, double 
     return {p_new, e_new, q_new, bvc, pbvc};
 }
 
+template <class M = IeeeOps>
+__device__ __forceinline__ EosOut eos_reps(const Params &P, double e_in, double delv_in,
+                                           double p_in, double q_in, double qq_in,
+                                           double ql_in, double vnewc, int rep)
+{
+    if (unit_refdens(P))
+        return eos_reps_rho<M, true>(P, e_in, delv_in, p_in, q_in, qq_in, ql_in, vnewc, rep);
+    return eos_reps_rho<M, false>(P, e_in, delv_in, p_in, q_in, qq_in, ql_in, vnewc, rep);
+}
+
 // CalcSoundSpeedForElems for one element (lulesh.cc:2180-2200).
 template <class M = IeeeOps>
 __device__ __forceinline__ double eos_sound_speed(const Params &P, const EosOut &o, double vnewc)
 {
-    return ssc_of<M>(M::ss_num(o.pbvc, o.e, vnewc, o.bvc, o.p), P.refdens);
+    const double num = M::ss_num(o.pbvc, o.e, vnewc, o.bvc, o.p);
+    if (unit_refdens(P)) return ssc_of<M, true>(num, P.refdens);
+    return ssc_of<M, false>(num, P.refdens);
 }
 
 // EvalEOSForElems for one element (lulesh.cc:2204-2324): the repetitions,

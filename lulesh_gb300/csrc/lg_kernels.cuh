@@ -470,13 +470,15 @@ __device__ __forceinline__ void material_finish(const DevState &s, const MatItem
         // CalcCourantConstraintForElems (2447-2513) and
         // CalcHydroConstraintForElems (2517-2572) for one element.  The
         // reference evaluates the Courant dt of every element but keeps it
-        // only where vdov != 0; a warp of elements at rest skips it.
-        const double vdov = s.vdov[ielem];
+        // only where vdov != 0; a warp of elements at rest skips it (the
+        // barriers keep the compiler from hoisting that work above the vote).
+        double vdov = s.vdov[ielem];
         const bool moving = dnz(vdov);
         if (__any_sync(__activemask(), moving) && moving) {
             const double qqc2 = 64.0 * P.qqc * P.qqc;
-            const double ssv = s.ss[ielem];
-            const double arealg = s.arealg[ielem];
+            double ssv = s.ss[ielem];
+            double arealg = s.arealg[ielem];
+            opaque(vdov); opaque(ssv); opaque(arealg);
             double dtf = ssv * ssv;
             if (dlt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
             dtf = sqrt(dtf);

@@ -395,12 +395,13 @@ __device__ __forceinline__ void material_element(const DevState &s, const int t,
     if (MODE != 0) {
         // Only elements with vdov != 0 constrain dt; a warp of elements at
         // rest skips the FP64 square root and reciprocals altogether.
-        const double vdov = s.vdov[ielem];
+        double vdov = s.vdov[ielem];
         const bool moving = ((unsigned long long)__double_as_longlong(vdov) << 1) != 0ull;
         if (__any_sync(__activemask(), moving) && moving) {
             const double qqc2 = 64.0 * P.qqc * P.qqc;
-            const double ssv = s.ss[ielem];
-            const double arealg = s.arealg[ielem];
+            double ssv = s.ss[ielem];
+            double arealg = s.arealg[ielem];
+            opaque(vdov); opaque(ssv); opaque(arealg);
             double dtf = ssv * ssv;
             if (FastOps::lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
             dtf = arealg * rcp_nr(sqrt_nr(dtf));
@@ -506,12 +507,13 @@ __device__ __forceinline__ void material_finish(const DevState &s, const MatItem
     if (MODE != 0) {
         // Only elements with vdov != 0 constrain dt; a warp of elements at
         // rest skips the FP64 square root and reciprocals altogether.
-        const double vdov = s.vdov[ielem];
+        double vdov = s.vdov[ielem];
         const bool moving = ((unsigned long long)__double_as_longlong(vdov) << 1) != 0ull;
         if (__any_sync(__activemask(), moving) && moving) {
             const double qqc2 = 64.0 * P.qqc * P.qqc;
-            const double ssv = s.ss[ielem];
-            const double arealg = s.arealg[ielem];
+            double ssv = s.ss[ielem];
+            double arealg = s.arealg[ielem];
+            opaque(vdov); opaque(ssv); opaque(arealg);
             double dtf = ssv * ssv;
             if (FastOps::lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
             dtf = arealg * rcp_nr(sqrt_nr(dtf));
