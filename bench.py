@@ -72,13 +72,13 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 # or not, since a warp instruction holds the pipe for the same time either
 # way) x 32 / units (elements; k_nodes: nodes), from ncu captures of the four
 # cycle kernels of the benchmark problem (s=150, 11 regions, balance 1, cost
-# 1) at cycle 10; captures at cycles 1 to 500 agree to 0.5 %
+# 1) at cycle 10; captures at cycles 1 to 500 agree to 0.7 %
 # (profiles/leapfrog_fp64_s150_counts.md).  The mixed build's counts are from
 # s=192, 16 regions, balance 2, cost 4 at cycle 10.
 FP64_SLOTS_PER_UNIT = {
     "fp64": {"k_forces": 1273, "k_nodes": 78, "k_kinematics": 700, "k_material": 420},
     "fp64-fma": {"k_forces": 785, "k_nodes": 72, "k_kinematics": 602, "k_material": 364},
-    "mixed": {"k_forces": 24, "k_nodes": 12, "k_kinematics": 95, "k_material": 606},
+    "mixed": {"k_forces": 24, "k_nodes": 12, "k_kinematics": 95, "k_material": 571},
 }
 # The workload (nx, regions, balance, cost) each build's counts were taken
 # with; k_material's depend on the region mix, the others on nothing.
