@@ -366,9 +366,35 @@ __device__ __forceinline__ void finish_dt(const DevState &s, double dtc, double 
     if (!am_last) return;
     __threadfence();
     double c = 1.0e+20, h = 1.0e+20;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-        c = dmin_sel(c, __ldcg(&s.dt_partial[2 * i]));
-        h = dmin_sel(h, __ldcg(&s.dt_partial[2 * i + 1]));
+    const int nb = (int)gridDim.x;
+    constexpr int kLanes = 8;
+    if (nb >= 4 * kLanes * BS) {
+        // A large grid: eight independent minima per thread, so that the
+        // loads of the partials overlap instead of waiting one after another
+        // (the minimum of exact values does not depend on the order).
+        double cu[kLanes], hu[kLanes];
+#pragma unroll
+        for (int u = 0; u < kLanes; ++u) cu[u] = hu[u] = 1.0e+20;
+        for (int i0 = threadIdx.x; i0 < nb; i0 += kLanes * BS) {
+#pragma unroll
+            for (int u = 0; u < kLanes; ++u) {
+                const int i = i0 + u * BS;
+                if (i < nb) {
+                    cu[u] = dmin_sel(cu[u], __ldcg(&s.dt_partial[2 * i]));
+                    hu[u] = dmin_sel(hu[u], __ldcg(&s.dt_partial[2 * i + 1]));
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kLanes; ++u) {
+            c = dmin_sel(c, cu[u]);
+            h = dmin_sel(h, hu[u]);
+        }
+    } else {
+        for (int i = threadIdx.x; i < nb; i += BS) {
+            c = dmin_sel(c, __ldcg(&s.dt_partial[2 * i]));
+            h = dmin_sel(h, __ldcg(&s.dt_partial[2 * i + 1]));
+        }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
