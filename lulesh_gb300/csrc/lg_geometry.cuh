@@ -4,8 +4,10 @@
 // the reference scales by powers of two, some functions apply the product of
 // those factors once (each says so); a power of two scales a rounded result
 // exactly, so with R = double and no contraction the values are the
-// reference's bit for bit.  node_normals_nozero and hourglass_modes regroup
-// sums and round differently; only the FMA build uses them.
+// reference's bit for bit.  node_normals_nozero, node_normals_x8,
+// area_face_cross (through char_length<R, true>) and hourglass_modes are
+// algebraically equal reformulations that round differently; only the FMA
+// build uses them.
 #pragma once
 
 #ifdef __CUDACC__
@@ -304,6 +306,43 @@ LG_HD void node_normals_nozero(R *pfx, R *pfy, R *pfz, const R *x, const R *y, c
 #undef LG_NN
 }
 
+// 8 x the node normals of CalcElemNodeNormals from the faces' diagonals: the
+// reference's bisectors of face (a, b, c, d) are (p + q) / 2 and (p - q) / 2
+// for p = r_c - r_a, q = r_d - r_b, so its area vector
+// 0.25 (p + q)/2 x (p - q)/2 equals (q x p) / 8 in exact arithmetic.  Each
+// node sums its three faces' q x p as node_normals_nozero does; the caller
+// applies the factor 1/8 (an exact power of two) once.  12 operations per
+// face instead of 27; the rounding differs from the reference's.
+template <typename R>
+LG_HD void node_normals_x8(R *pfx, R *pfy, R *pfz, const R *x, const R *y, const R *z)
+{
+    R ax[6], ay[6], az[6];
+    constexpr int F[6][4] = {{0, 1, 2, 3}, {0, 4, 5, 1}, {1, 5, 6, 2},
+                             {2, 6, 7, 3}, {3, 7, 4, 0}, {4, 7, 6, 5}};
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        const int a = F[f][0], b = F[f][1], c = F[f][2], d = F[f][3];
+        const R px = x[c] - x[a], py = y[c] - y[a], pz = z[c] - z[a];
+        const R qx = x[d] - x[b], qy = y[d] - y[b], qz = z[d] - z[b];
+        ax[f] = qy * pz - qz * py;
+        ay[f] = qz * px - qx * pz;
+        az[f] = qx * py - qy * px;
+    }
+#define LG_NN(P, A)                                 \
+    P[0] = (A[0] + A[1]) + A[4];                    \
+    P[1] = (A[0] + A[1]) + A[2];                    \
+    P[2] = (A[0] + A[2]) + A[3];                    \
+    P[3] = (A[0] + A[3]) + A[4];                    \
+    P[4] = (A[1] + A[4]) + A[5];                    \
+    P[5] = (A[1] + A[2]) + A[5];                    \
+    P[6] = (A[2] + A[3]) + A[5];                    \
+    P[7] = (A[3] + A[4]) + A[5];
+    LG_NN(pfx, ax)
+    LG_NN(pfy, ay)
+    LG_NN(pfz, az)
+#undef LG_NN
+}
+
 // The four hourglass mode sums sum_k gam(m, k) * v[k] of CalcFBHourglassForceForElems
 // (lulesh.cc:894-920) by a pairwise butterfly: 18 additions instead of 28.
 // The FMA build uses it; it rounds differently from the left-to-right sums.
@@ -403,11 +442,37 @@ LG_HD R area_face(const R *x, const R *y, const R *z, int a, int b, int c,
            (fx * gx + fy * gy + fz * gz) * (fx * gx + fy * gy + fz * gz);
 }
 
-// CalcElemCharacteristicLength, lulesh.cc:1394-1435 (std::max(a,b) is
-// (a < b) ? b : a)
+// A quarter of AreaFace from the face's diagonals p = r_c - r_a and
+// q = r_d - r_b: with f = p - q and g = p + q, |f|^2 |g|^2 - (f.g)^2 equals
+// 4 |p x q|^2 in exact arithmetic.  15 operations instead of 23; the
+// rounding differs from the reference's expression.
 template <typename R>
+LG_HD R area_face_cross(const R *x, const R *y, const R *z, int a, int b, int c, int d)
+{
+    const R px = x[c] - x[a], py = y[c] - y[a], pz = z[c] - z[a];
+    const R qx = x[d] - x[b], qy = y[d] - y[b], qz = z[d] - z[b];
+    const R cx = py * qz - pz * qy, cy = pz * qx - px * qz, cz = px * qy - py * qx;
+    return cx * cx + cy * cy + cz * cz;
+}
+
+// CalcElemCharacteristicLength, lulesh.cc:1394-1435 (std::max(a,b) is
+// (a < b) ? b : a).  kCross (the FMA build) takes the face areas from
+// area_face_cross: the maximum of a quarter of each area, and
+// 4 v / sqrt(4 m) = 2 v / sqrt(m) exactly, since the factor 4 only shifts
+// exponents.
+template <typename R, bool kCross = false>
 LG_HD R char_length(const R *x, const R *y, const R *z, R volume)
 {
+    if (kCross) {
+        R m = R(0.0), a;
+        a = area_face_cross(x, y, z, 0, 1, 2, 3); m = lt(a, m) ? m : a;
+        a = area_face_cross(x, y, z, 4, 5, 6, 7); m = lt(a, m) ? m : a;
+        a = area_face_cross(x, y, z, 0, 1, 5, 4); m = lt(a, m) ? m : a;
+        a = area_face_cross(x, y, z, 1, 2, 6, 5); m = lt(a, m) ? m : a;
+        a = area_face_cross(x, y, z, 2, 3, 7, 6); m = lt(a, m) ? m : a;
+        a = area_face_cross(x, y, z, 3, 0, 4, 7); m = lt(a, m) ? m : a;
+        return R(2.0) * volume / sqrt(m);
+    }
     R cl = R(0.0), a;
     a = area_face(x, y, z, 0, 1, 2, 3); cl = lt(a, cl) ? cl : a;
     a = area_face(x, y, z, 4, 5, 6, 7); cl = lt(a, cl) ? cl : a;

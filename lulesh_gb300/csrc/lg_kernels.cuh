@@ -43,12 +43,12 @@
 #ifndef LG_NS
 #error "define LG_NS"
 #endif
-// LG_REASSOC (the FMA build): the hourglass and node-normal sums are
-// regrouped to save FP64 instructions (node_normals_nozero, the
-// hourglass_modes butterfly, and the 1/12 and 1/volume factors applied once
-// per mode instead of once per term).  The rounding differs from the
-// reference's operand order, as FMA contraction's does; the parity bar
-// covers both.
+// LG_REASSOC (the FMA build): algebraically equal forms that save FP64
+// instructions: node normals and face areas from the faces' diagonals
+// (node_normals_x8, area_face_cross), the hourglass_modes butterfly, and the
+// 1/12 and 1/volume factors applied once per mode instead of once per term.
+// The rounding differs from the reference's operand order, as FMA
+// contraction's does; the parity bar covers both.
 #ifndef LG_REASSOC
 #define LG_REASSOC 0
 #endif
@@ -83,11 +83,13 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
 
     // InitStressTermsForElems (273-286) + IntegrateStressForElems (494-587)
     {
-        const double sig = -s.p[k] - s.q[k];
         double pfx[8], pfy[8], pfz[8];
 #if LG_REASSOC
-        node_normals_nozero(pfx, pfy, pfz, x, y, z);
+        // 8 x the normals; the 1/8 goes into sig (exact)
+        const double sig = (-s.p[k] - s.q[k]) * 0.125;
+        node_normals_x8(pfx, pfy, pfz, x, y, z);
 #else
+        const double sig = -s.p[k] - s.q[k];
         node_normals(pfx, pfy, pfz, x, y, z);
 #endif
 #pragma unroll
@@ -304,7 +306,7 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
     const double relativeVolume = volume / volo;
     s.vnew[k] = relativeVolume;
     s.delv[k] = relativeVolume - s.v[k];
-    s.arealg[k] = char_length(x, y, z, volume);
+    s.arealg[k] = char_length<double, LG_REASSOC != 0>(x, y, z, volume);
     {
         const double dt2 = 0.5 * ctl->deltatime;
         double xh[8], yh[8], zh[8];

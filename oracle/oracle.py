@@ -174,8 +174,8 @@ class OracleDomain:
         return out
 
 
-def _ref() -> ctypes.CDLL:
-    lib = _load(REF_LIB)
+def _ref(path: str = REF_LIB) -> ctypes.CDLL:
+    lib = _load(path)
     lib.ref_create.restype = ctypes.c_void_p
     lib.ref_create.argtypes = [ctypes.c_int] * 4 + [ctypes.c_double] * 2
     lib.ref_destroy.argtypes = [ctypes.c_void_p]
@@ -200,8 +200,8 @@ class RefDomain:
     """The reference's own Domain and timestep (unchanged sources)."""
 
     def __init__(self, nx: int, numReg: int = 11, balance: int = 1, cost: int = 1,
-                 hgcoef: float = 3.0, einit_factor: float = 1.0):
-        self._lib = _ref()
+                 hgcoef: float = 3.0, einit_factor: float = 1.0, lib_path: str = REF_LIB):
+        self._lib = _ref(lib_path)
         self._h = self._lib.ref_create(nx, numReg, balance, cost, hgcoef, einit_factor)
         self.nx = nx
 
