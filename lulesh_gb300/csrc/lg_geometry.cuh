@@ -193,18 +193,11 @@ LG_HD R shape_derivs(const R *x, const R *y, const R *z, R bx[4], R by[4],
 // determinant and fills 64 x rows 0..3 of B.  A velocity gradient formed as
 // (1 / det) * (B . v) from these equals the one formed from shape_derivs bit
 // for bit, since only powers of two were dropped and they cancel exactly.
+// The cofactor part of shape_derivs_x64 from 8 x the Jacobian's columns.
 template <typename R>
-LG_HD R shape_derivs_x64(const R *x, const R *y, const R *z, R bx[4], R by[4], R bz[4])
+LG_HD R shape_derivs_x64_jac(R fjxxi, R fjxet, R fjxze, R fjyxi, R fjyet, R fjyze, R fjzxi,
+                             R fjzet, R fjzze, R bx[4], R by[4], R bz[4])
 {
-    const R fjxxi = ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
-    const R fjxet = ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
-    const R fjxze = ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
-    const R fjyxi = ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
-    const R fjyet = ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
-    const R fjyze = ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
-    const R fjzxi = ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
-    const R fjzet = ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
-    const R fjzze = ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
     const R cjxxi = (fjyet * fjzze) - (fjzet * fjyze);
     const R cjxet = -(fjyxi * fjzze) + (fjzxi * fjyze);
     const R cjxze = (fjyxi * fjzet) - (fjzxi * fjyet);
@@ -227,6 +220,22 @@ LG_HD R shape_derivs_x64(const R *x, const R *y, const R *z, R bx[4], R by[4], R
     bz[2] = cjzxi + cjzet - cjzze;
     bz[3] = -cjzxi + cjzet - cjzze;
     return fjxet * cjxet + fjyet * cjyet + fjzet * cjzet;
+}
+
+template <typename R>
+LG_HD R shape_derivs_x64(const R *x, const R *y, const R *z, R bx[4], R by[4], R bz[4])
+{
+    const R fjxxi = ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxet = ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
+    const R fjxze = ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
+    const R fjyxi = ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyet = ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
+    const R fjyze = ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
+    const R fjzxi = ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzet = ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
+    const R fjzze = ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
+    return shape_derivs_x64_jac(fjxxi, fjxet, fjxze, fjyxi, fjyet, fjyze, fjzxi, fjzet, fjzze,
+                                bx, by, bz);
 }
 
 // Area vector of SumElemFaceNormal, lulesh.cc:381-415 (the four corners
@@ -304,6 +313,67 @@ LG_HD void node_normals_nozero(R *pfx, R *pfy, R *pfz, const R *x, const R *y, c
     LG_NN(pfy, ay)
     LG_NN(pfz, az)
 #undef LG_NN
+}
+
+// Body diagonals r6 - r0, r5 - r3, r7 - r1, r4 - r2 of one coordinate.
+template <typename R>
+LG_HD void body_diagonals(const R *a, R D[4])
+{
+    D[0] = a[6] - a[0];
+    D[1] = a[5] - a[3];
+    D[2] = a[7] - a[1];
+    D[3] = a[4] - a[2];
+}
+
+// An element's xi, eta and zeta differences of one coordinate from its body
+// diagonals D: 8 x a column of CalcElemShapeFunctionDerivatives' Jacobian
+// (lulesh.cc:304-316 without the factor 1/8) and 4 x the differences of
+// CalcMonotonicQGradientsForElems (lulesh.cc:1650-1706 without the 1/4),
+// xi = D0 + D1 - D2 - D3, eta = D0 - D1 + D2 - D3, zeta = D0 + D1 + D2 + D3.
+// 7 operations for the three, where the node sums take 21; the rounding
+// differs from the reference's sums.
+template <typename R>
+LG_HD void diag_directions(const R D[4], R &xi, R &et, R &ze)
+{
+    const R s = D[0] + D[1], t = D[2] + D[3], u = D[0] - D[1], w = D[2] - D[3];
+    xi = s - t;
+    et = u + w;
+    ze = s + t;
+}
+
+// CalcMonotonicQGradientsForElems for one element from the body diagonals of
+// its coordinates (Dx, Dy, Dz) and velocities (Ex, Ey, Ez), with the powers of
+// two folded as in monoq_gradients<R, true>.
+template <typename R>
+LG_HD void monoq_gradients_diag(const R *Dx, const R *Dy, const R *Dz, const R *Ex, const R *Ey,
+                                const R *Ez, R vol, R out[6])
+{
+    const R ptiny_s = R(256.e-36);
+    const R norm = (R(1.0) / (vol + R(1.e-36))) * R(0.015625);
+    const R vol_s = R(16.0) * vol;
+    R dxi, dxj, dxk, dyi, dyj, dyk, dzi, dzj, dzk, vxi, vxj, vxk, vyi, vyj, vyk, vzi, vzj, vzk;
+    diag_directions(Dx, dxi, dxj, dxk);
+    diag_directions(Dy, dyi, dyj, dyk);
+    diag_directions(Dz, dzi, dzj, dzk);
+    diag_directions(Ex, vxi, vxj, vxk);
+    diag_directions(Ey, vyi, vyj, vyk);
+    diag_directions(Ez, vzi, vzj, vzk);
+    R ax, ay, az;
+    ax = dyi * dzj - dzi * dyj;
+    ay = dzi * dxj - dxi * dzj;
+    az = dxi * dyj - dyi * dxj;
+    out[2] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
+    out[5] = (ax * norm) * vxk + (ay * norm) * vyk + (az * norm) * vzk;
+    ax = dyj * dzk - dzj * dyk;
+    ay = dzj * dxk - dxj * dzk;
+    az = dxj * dyk - dyj * dxk;
+    out[0] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
+    out[3] = (ax * norm) * vxi + (ay * norm) * vyi + (az * norm) * vzi;
+    ax = dyk * dzi - dzk * dyi;
+    ay = dzk * dxi - dxk * dzi;
+    az = dxk * dyi - dyk * dxi;
+    out[1] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
+    out[4] = (ax * norm) * vxj + (ay * norm) * vyj + (az * norm) * vzj;
 }
 
 // 8 x the node normals of CalcElemNodeNormals from the faces' diagonals: the

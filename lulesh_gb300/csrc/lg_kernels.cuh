@@ -307,6 +307,45 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
     s.vnew[k] = relativeVolume;
     s.delv[k] = relativeVolume - s.v[k];
     s.arealg[k] = char_length<double, LG_REASSOC != 0>(x, y, z, volume);
+#if LG_REASSOC
+    // The velocity gradient's Jacobian, the half-step coordinates and the
+    // monotonic-Q differences all from the element's body diagonals
+    // (diag_directions): 8 x the Jacobian at x - dt/2 v, the velocity terms
+    // v0 - v6, v1 - v7, v2 - v4, v3 - v5 as -E0, -E2, -E3, -E1.
+    double Dx[4], Dy[4], Dz[4], Ex[4], Ey[4], Ez[4];
+    body_diagonals(x, Dx);
+    body_diagonals(y, Dy);
+    body_diagonals(z, Dz);
+    body_diagonals(xv, Ex);
+    body_diagonals(yv, Ey);
+    body_diagonals(zv, Ez);
+    {
+        const double dt2 = 0.5 * ctl->deltatime;
+        double Hx[4], Hy[4], Hz[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            Hx[j] = Dx[j] - dt2 * Ex[j];
+            Hy[j] = Dy[j] - dt2 * Ey[j];
+            Hz[j] = Dz[j] - dt2 * Ez[j];
+        }
+        double fxi, fxe, fxz, fyi, fye, fyz, fzi, fze, fzz;
+        diag_directions(Hx, fxi, fxe, fxz);
+        diag_directions(Hy, fyi, fye, fyz);
+        diag_directions(Hz, fzi, fze, fzz);
+        double bx[4], by[4], bz[4];
+        const double inv_detJ =
+            1.0 / shape_derivs_x64_jac(fxi, fxe, fxz, fyi, fye, fyz, fzi, fze, fzz, bx, by, bz);
+        const double dxx = -inv_detJ * (bx[0] * Ex[0] + bx[1] * Ex[2] + bx[2] * Ex[3] + bx[3] * Ex[1]);
+        const double dyy = -inv_detJ * (by[0] * Ey[0] + by[1] * Ey[2] + by[2] * Ey[3] + by[3] * Ey[1]);
+        const double dzz = -inv_detJ * (bz[0] * Ez[0] + bz[1] * Ez[2] + bz[2] * Ez[3] + bz[3] * Ez[1]);
+        s.vdov[k] = dxx + dyy + dzz;
+    }
+    if (relativeVolume <= 0.0) raise_status(ctl, -1);  // lulesh.cc:1598-1605
+
+    // CalcMonotonicQGradientsForElems
+    double g[6];
+    monoq_gradients_diag(Dx, Dy, Dz, Ex, Ey, Ez, volo * relativeVolume, g);
+#else
     {
         const double dt2 = 0.5 * ctl->deltatime;
         double xh[8], yh[8], zh[8];
@@ -316,16 +355,10 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
             yh[j] = y[j] - dt2 * yv[j];
             zh[j] = z[j] - dt2 * zv[j];
         }
-        // Strict build: 64 x the determinant and 64 x B, whose factors cancel
-        // exactly in inv_detJ * (B . v).  The FMA build keeps the reference's
-        // formulation: with contraction the two are not bitwise equal, and
-        // its parity margin was measured with this one.
+        // 64 x the determinant and 64 x B, whose factors cancel exactly in
+        // inv_detJ * (B . v)
         double bx[4], by[4], bz[4];
-#if LG_REASSOC
-        const double inv_detJ = 1.0 / shape_derivs(xh, yh, zh, bx, by, bz);
-#else
         const double inv_detJ = 1.0 / shape_derivs_x64(xh, yh, zh, bx, by, bz);
-#endif
         const double dxx = inv_detJ * (bx[0] * (xv[0] - xv[6]) + bx[1] * (xv[1] - xv[7]) +
                                        bx[2] * (xv[2] - xv[4]) + bx[3] * (xv[3] - xv[5]));
         const double dyy = inv_detJ * (by[0] * (yv[0] - yv[6]) + by[1] * (yv[1] - yv[7]) +
@@ -338,7 +371,8 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
 
     // CalcMonotonicQGradientsForElems
     double g[6];
-    monoq_gradients<double, !LG_REASSOC>(x, y, z, xv, yv, zv, volo * relativeVolume, g);
+    monoq_gradients<double, true>(x, y, z, xv, yv, zv, volo * relativeVolume, g);
+#endif
     s.delx_xi[k] = g[0];
     s.delx_eta[k] = g[1];
     s.delx_zeta[k] = g[2];

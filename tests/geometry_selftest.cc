@@ -114,6 +114,39 @@ int main(int argc, char **argv)
         const double cl = geo_ref_char_length(x, y, z, vol);
         near("char_length from diagonals", cl, char_length<double, true>(x, y, z, vol),
              1e-12 * std::fabs(cl));
+
+        // the velocity gradient from the body diagonals (at dt = 0 the
+        // half-step diagonals are the coordinates' own)
+        double Dx[4], Dy[4], Dz[4], Ex[4], Ey[4], Ez[4];
+        body_diagonals(x, Dx);
+        body_diagonals(y, Dy);
+        body_diagonals(z, Dz);
+        body_diagonals(xv, Ex);
+        body_diagonals(yv, Ey);
+        body_diagonals(zv, Ez);
+        double fxi, fxe, fxz, fyi, fye, fyz, fzi, fze, fzz;
+        diag_directions(Dx, fxi, fxe, fxz);
+        diag_directions(Dy, fyi, fye, fyz);
+        diag_directions(Dz, fzi, fze, fzz);
+        const double invd =
+            1.0 / shape_derivs_x64_jac(fxi, fxe, fxz, fyi, fye, fyz, fzi, fze, fzz, bx, by, bz);
+        const double cond = omax / h;  // the reference's node sums lose this factor
+        const double tol_g = 256 * 2.220446049250313e-16 * cond * cond / h;
+        near("dxx from diagonals", grad(inv, b, xv),
+             -invd * (bx[0] * Ex[0] + bx[1] * Ex[2] + bx[2] * Ex[3] + bx[3] * Ex[1]), tol_g);
+        near("dyy from diagonals", grad(inv, b + 8, yv),
+             -invd * (by[0] * Ey[0] + by[1] * Ey[2] + by[2] * Ey[3] + by[3] * Ey[1]), tol_g);
+        near("dzz from diagonals", grad(inv, b + 16, zv),
+             -invd * (bz[0] * Ez[0] + bz[1] * Ez[2] + bz[2] * Ez[3] + bz[3] * Ez[1]), tol_g);
+
+        // the monotonic-Q gradients from the body diagonals
+        double gref[6], gdia[6];
+        monoq_gradients<double, false>(x, y, z, xv, yv, zv, vol, gref);
+        monoq_gradients_diag(Dx, Dy, Dz, Ex, Ey, Ez, vol, gdia);
+        for (int c = 0; c < 3; ++c)
+            near("delx from diagonals", gref[c], gdia[c], 256 * 2.220446049250313e-16 * cond * h);
+        for (int c = 3; c < 6; ++c)
+            near("delv from diagonals", gref[c], gdia[c], 256 * 2.220446049250313e-16 * cond * cond);
     }
 
     // the FP32 sign filter of the Jacobian determinant: it may only claim
