@@ -333,7 +333,7 @@ __device__ __forceinline__ double dmin_sel(double a, double b) { return (b < a) 
 // Reduces (dtc, dth) over the block; the last block of the grid reduces the
 // per-block results into ctl->dtcourant/dthydro, merges error flags and, if
 // advance, evaluates the loop condition and TimeIncrement of the next cycle.
-template <int BS>
+template <int BS, bool kUnrolledFold = false>
 __device__ __forceinline__ void finish_dt(const DevState &s, double dtc, double dth, bool advance)
 {
     __shared__ double red[2][BS / 32];
@@ -368,10 +368,13 @@ __device__ __forceinline__ void finish_dt(const DevState &s, double dtc, double 
     double c = 1.0e+20, h = 1.0e+20;
     const int nb = (int)gridDim.x;
     constexpr int kLanes = 8;
-    if (nb >= 4 * kLanes * BS) {
+    if (kUnrolledFold && nb >= 4 * kLanes * BS) {
         // A large grid: eight independent minima per thread, so that the
         // loads of the partials overlap instead of waiting one after another
-        // (the minimum of exact values does not depend on the order).
+        // (the minimum of exact values does not depend on the order).  Only
+        // the FP64 kernels take it: in the mixed path's k_material the same
+        // fold measured 1.5 ms slower per launch at s=192, for a cause not
+        // found, while it saves 64 us in the FP64 one at s=150.
         double cu[kLanes], hu[kLanes];
 #pragma unroll
         for (int u = 0; u < kLanes; ++u) cu[u] = hu[u] = 1.0e+20;

@@ -622,7 +622,7 @@ __global__ void __launch_bounds__(BS) k_material_finish(DevState s)
         material_finish<MODE>(s, m, o, dtc, dth);
     }
     if (MODE != 0)
-        finish_dt<BS>(s, dtc, dth, MODE == 2);
+        finish_dt<BS, true>(s, dtc, dth, MODE == 2);
     else
         finish_material_flags(s);
 }
@@ -640,7 +640,7 @@ __global__ void __launch_bounds__(BS) k_material(DevState s)
         if (t < s.nItems && material_load<MODE>(s, t, s.ctl, m))
             material_update<MODE>(s, m, dtc, dth);
         if (MODE != 0)
-            finish_dt<BS>(s, dtc, dth, MODE == 2);
+            finish_dt<BS, true>(s, dtc, dth, MODE == 2);
         else
             finish_material_flags(s);
         return;
