@@ -324,10 +324,9 @@ int lg_halo_unpack(lg_halo_plan *plan, double *const *fields, const double *recv
  * scratch is one fixed static device array of 48 doubles per element for at
  * most 32768 elements (about 12.6 MB, held on every GPU where the call has
  * run until the process exits); larger meshes are rejected with
- * LG_ERR_INVALID.  The first call on each device looks up that array's
- * device address; make that first call before any stream capture on the
- * device.  Every call reads its status word back and so blocks the host
- * until its kernels have finished.  A non-sticky CUDA error left pending by
+ * LG_ERR_INVALID.  Every call copies its status word back and synchronises
+ * the stream, so it blocks the host until its kernels have finished and no
+ * call can be captured into a CUDA graph.  A non-sticky CUDA error left pending by
  * the caller's earlier work is cleared on entry, so that a failure reported
  * here is this call's own.  All calls share the array: calls whose work
  * overlaps on one GPU race and must be serialised by the caller. */
