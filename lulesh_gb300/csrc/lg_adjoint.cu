@@ -87,11 +87,22 @@ __global__ void __launch_bounds__(kB) ka_gather(lg::DevState s, AdjArgs a)
     if (n < s.N) adj_gather(s, a, n);
 }
 
-__global__ void ka_hg_sum(const double *part, int nparts, double *acc)
+// Adds the per-block hourglass-coefficient partials of one reverse cycle to
+// acc: one block, each thread summing a strided subset in index order, then
+// a pairwise tree in shared memory.  The order is fixed, so the sum is the
+// same on every run; one thread reading them in turn waited on each load.
+__global__ void __launch_bounds__(kB) ka_hg_sum(const double *part, int nparts, double *acc)
 {
+    __shared__ double red[kB];
     double t = 0.;
-    for (int i = 0; i < nparts; ++i) t += part[i];
-    *acc += t;
+    for (int i = threadIdx.x; i < nparts; i += kB) t += part[i];
+    red[threadIdx.x] = t;
+    __syncthreads();
+    for (int w = kB / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *acc += red[0];
 }
 
 int err(int code, const char *fmt, ...)
@@ -327,7 +338,7 @@ int adjoint_run(const AdjointIO &io, double *J, double *dJdhg)
             ka_nodes<<<nbk, kB, 0, st>>>(S, A);
             ka_forces<<<eb, kB, 0, st>>>(S, A);
             ka_gather<<<nbk, kB, 0, st>>>(S, A);
-            ka_hg_sum<<<1, 1, 0, st>>>(hgPart, eb, hgAcc);
+            ka_hg_sum<<<1, kB, 0, st>>>(hgPart, eb, hgAcc);
         }
         AD_CUDA(cudaGetLastError());
     }

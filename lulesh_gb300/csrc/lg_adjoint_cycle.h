@@ -185,7 +185,7 @@ LG_HD void adj_kinematics(const DevState &s, const AdjArgs &a, const int k)
     const double vnewb = a.vnewb[k] + adj::qgrad_vjp(x, y, z, xd, yd, zd, volo, vnew, dxb, dvb, xb,
                                                      yb, zb, xdb, ydb, zdb);
     // vnew = V(x) / volo, dV/dx = CalcElemVolumeDerivative
-    const double Vb = vnewb / volo;
+    const double Vb = vnewb * (1.0 / volo);  // vnewb is 0 for most elements
     double dvdx[8], dvdy[8], dvdz[8];
     geom::volume_derivative(x, y, z, dvdx, dvdy, dvdz);
 #pragma unroll

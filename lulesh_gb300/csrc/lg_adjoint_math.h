@@ -266,7 +266,9 @@ LG_HD void forces_vjp(const double *x, const double *y, const double *z, const d
     // coef = -hg 0.01 ss mass vol^(-1/3); volinv = 1 / vol; vol = volo v
     o.hgb += coefb * (-0.01 * ss * mass / cr);
     o.ssb += coefb * (-hg * 0.01 * mass / cr);
-    double volb = coefb * coef * (-1.0 / 3.0) / vol;
+    // the divisions take forward values: an adjoint dividend is 0 for most
+    // elements, and a zero dividend takes division's special-operand path
+    double volb = coefb * (coef * (-1.0 / 3.0) / vol);
     volb -= volinvb * volinv * volinv;
     o.vb += volb * volo;
 }
@@ -331,8 +333,9 @@ LG_HD double qgrad_vjp(const double *x, const double *y, const double *z, const 
         const V3 a = cross(*Ps[d], *Qs[d]);
         const double s = sqrt(dot(a, a) + ptiny);
         const double gx = delxb[d], gv = delvb[d];
-        volb += gx / s;
-        const double ka = -gx * vol / (s * s * s);
+        const double rs = 1.0 / s;  // gx, an adjoint, is 0 for most elements
+        volb += gx * rs;
+        const double ka = -gx * (vol * (rs * rs * rs));
         V3 ab = {ka * a.x + gv * norm * Vs[d]->x, ka * a.y + gv * norm * Vs[d]->y,
                  ka * a.z + gv * norm * Vs[d]->z};
         normb += gv * dot(a, *Vs[d]);
@@ -439,11 +442,29 @@ struct EosFwd {
         sscFsqrt, qn2keep, sssqrt, comp_gt;
 };
 
+// Keeps the compiler from moving the computation of v out of the branch it
+// sits in (on the device; nothing on the host).  A hoisted square root or
+// division runs for every element, and an element at rest gives it the
+// operands of the special-operand path (a zero numerator).
+LG_HD void adj_fence(double &v)
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("" : "+d"(v));
+#else
+    (void)v;
+#endif
+}
+
+// The sound-speed term; kUnitRho (refdens == 1, decided once by the caller)
+// skips x / 1.0, which is x.
+template <bool kUnitRho>
 LG_HD double ssc_val(double num, double rho0, bool &took_sqrt)
 {
-    double ssc = num / rho0;
+    double ssc = kUnitRho ? num : num / rho0;
     took_sqrt = !(ssc <= .1111111e-36);
-    return took_sqrt ? sqrt(ssc) : .3333333e-18;
+    if (!took_sqrt) return .3333333e-18;
+    adj_fence(ssc);
+    return sqrt(ssc);
 }
 
 // pressure with its cut-off and clamps; keep = the derivative passes (the
@@ -458,8 +479,9 @@ LG_HD double p_eval(const EosConst &K, double bvc, double e, double vc, bool &ke
     return p;
 }
 
-LG_HD EosFwd eos_forward(const EosConst &K, double e_old, double delvc, double p_old,
-                         double q_old, double qq, double ql, double vc)
+template <bool kUnitRho>
+LG_HD EosFwd eos_forward_rho(const EosConst &K, double e_old, double delvc, double p_old,
+                             double q_old, double qq, double ql, double vc)
 {
     EosFwd f;
     const double c1s = 2.0 / 3.0, sixth = 1.0 / 6.0;
@@ -482,7 +504,7 @@ LG_HD EosFwd eos_forward(const EosConst &K, double e_old, double delvc, double p
         f.sscH = 0.;
         f.sscHsqrt = false;
     } else {
-        f.sscH = ssc_val(c1s * f.e1 + f.vhalf * f.vhalf * f.bvcH * f.pH, K.rho0, f.sscHsqrt);
+        f.sscH = ssc_val<kUnitRho>(c1s * f.e1 + f.vhalf * f.vhalf * f.bvcH * f.pH, K.rho0, f.sscHsqrt);
         f.qn1 = f.sscH * ql + qq;
     }
     f.e2 = f.e1 + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (f.pH + f.qn1));
@@ -497,7 +519,7 @@ LG_HD EosFwd eos_forward(const EosConst &K, double e_old, double delvc, double p
         f.sscT = 0.;
         f.sscTsqrt = false;
     } else {
-        f.sscT = ssc_val(c1s * f.e3 + vc * vc * f.bvc * f.pn1, K.rho0, f.sscTsqrt);
+        f.sscT = ssc_val<kUnitRho>(c1s * f.e3 + vc * vc * f.bvc * f.pn1, K.rho0, f.sscTsqrt);
         f.qt = f.sscT * ql + qq;
     }
     f.e4 = f.e3 - (7.0 * (p_old + q_old) - 8.0 * (f.pH + f.qn1) + (f.pn1 + f.qt)) * delvc * sixth;
@@ -510,13 +532,20 @@ LG_HD EosFwd eos_forward(const EosConst &K, double e_old, double delvc, double p
     f.sscF = 0.;
     f.sscFsqrt = false;
     if (!f.comp_gt) {
-        f.sscF = ssc_val(c1s * f.e4 + vc * vc * f.bvc * f.pn2, K.rho0, f.sscFsqrt);
+        f.sscF = ssc_val<kUnitRho>(c1s * f.e4 + vc * vc * f.bvc * f.pn2, K.rho0, f.sscFsqrt);
         f.qn2 = f.sscF * ql + qq;
         f.qn2keep = true;
         if (fabs(f.qn2) < K.q_cut) f.qn2 = 0.;
     }
-    f.ss = ssc_val(c1s * f.e4 + vc * vc * f.bvc * f.pn2, K.rho0, f.sssqrt);
+    f.ss = ssc_val<kUnitRho>(c1s * f.e4 + vc * vc * f.bvc * f.pn2, K.rho0, f.sssqrt);
     return f;
+}
+
+LG_HD EosFwd eos_forward(const EosConst &K, double e_old, double delvc, double p_old,
+                         double q_old, double qq, double ql, double vc)
+{
+    if (K.rho0 == 1.0) return eos_forward_rho<true>(K, e_old, delvc, p_old, q_old, qq, ql, vc);
+    return eos_forward_rho<false>(K, e_old, delvc, p_old, q_old, qq, ql, vc);
 }
 
 struct EosAdj {
@@ -536,7 +565,7 @@ LG_HD EosAdj eos_vjp(const EosConst &K, const EosFwd &f, double e_old, double de
     double e4b = eb, pn2b = pb, bvcb = 0.;
     // ss = sqrt((c1s e4 + vc^2 bvc pn2) / rho0)
     if (f.sssqrt) {
-        const double nb = ssb / (2. * f.ss * r0);
+        const double nb = ssb * (1.0 / (2. * f.ss * r0));
         e4b += nb * c1s;
         a.vcb += nb * 2. * vc * f.bvc * f.pn2;
         bvcb += nb * vc * vc * f.pn2;
@@ -548,7 +577,7 @@ LG_HD EosAdj eos_vjp(const EosConst &K, const EosFwd &f, double e_old, double de
         a.qlb += qb * f.sscF;
         a.qqb += qb;
         if (f.sscFsqrt) {
-            const double nb = sb / (2. * f.sscF * r0);
+            const double nb = sb * (1.0 / (2. * f.sscF * r0));
             e4b += nb * c1s;
             a.vcb += nb * 2. * vc * f.bvc * f.pn2;
             bvcb += nb * vc * vc * f.pn2;
@@ -580,7 +609,7 @@ LG_HD EosAdj eos_vjp(const EosConst &K, const EosFwd &f, double e_old, double de
         a.qlb += qtb * f.sscT;
         a.qqb += qtb;
         if (f.sscTsqrt) {
-            const double nb = qtb * ql / (2. * f.sscT * r0);
+            const double nb = qtb * ql * (1.0 / (2. * f.sscT * r0));
             e3b += nb * c1s;
             a.vcb += nb * 2. * vc * f.bvc * f.pn1;
             bvcb += nb * vc * vc * f.pn1;
@@ -608,7 +637,7 @@ LG_HD EosAdj eos_vjp(const EosConst &K, const EosFwd &f, double e_old, double de
         a.qlb += qn1b * f.sscH;
         a.qqb += qn1b;
         if (f.sscHsqrt) {
-            const double nb = qn1b * ql / (2. * f.sscH * r0);
+            const double nb = qn1b * ql * (1.0 / (2. * f.sscH * r0));
             e1b += nb * c1s;
             vhalfb += nb * 2. * f.vhalf * f.bvcH * f.pH;
             bvcHb += nb * f.vhalf * f.vhalf * f.pH;
@@ -638,12 +667,14 @@ LG_HD EosAdj eos_vjp(const EosConst &K, const EosFwd &f, double e_old, double de
         compb += chsb;  // compHalfStep = compression
         chsb = 0.;
     }
-    // chs = 1 / (vc - 0.5 delvc) - 1; comp = 1 / vc - 1
+    // chs = 1 / (vc - 0.5 delvc) - 1; comp = 1 / vc - 1.  By reciprocals:
+    // at rest chsb and compb are 0, and a zero dividend would send a division
+    // down its special-operand path.
     const double vchalf = vc - delvc * .5;
-    const double vchb = -chsb / (vchalf * vchalf);
+    const double vchb = -chsb * (1.0 / (vchalf * vchalf));
     a.vcb += vchb;
     a.delvcb += -.5 * vchb;
-    a.vcb += -compb / (vc * vc);
+    a.vcb += -compb * (1.0 / (vc * vc));
     return a;
 }
 

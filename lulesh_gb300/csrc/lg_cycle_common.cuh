@@ -243,8 +243,8 @@ __device__ __forceinline__ EosOut eos_reps_rho(const Params &P, double e_in, dou
         double compression = M::div(1., vc) - 1.;
         const double vchalf = vc - delvc * .5;
         double compHalfStep = M::div(1., vchalf) - 1.;
-        if (P.eosvmin != 0. && M::le(vc, P.eosvmin)) compHalfStep = compression;
-        if (P.eosvmax != 0. && M::le(P.eosvmax, vc)) {
+        if (dnz(P.eosvmin) && M::le(vc, P.eosvmin)) compHalfStep = compression;
+        if (dnz(P.eosvmax) && M::le(P.eosvmax, vc)) {
             p_old = 0.;
             compression = 0.;
             compHalfStep = 0.;
@@ -328,7 +328,9 @@ __device__ __forceinline__ void eval_eos(const Params &P, double e_in, double de
     ss_out = need_ss ? eos_sound_speed<M>(P, o, vnewc) : 0.0;
 }
 
-__device__ __forceinline__ double dmin_sel(double a, double b) { return (b < a) ? b : a; }
+// min(a, b) as (b < a) ? b : a, the comparison on the integer pipe (dlt): the
+// block and grid reductions of the dt candidates run it ten times per thread
+__device__ __forceinline__ double dmin_sel(double a, double b) { return dlt(b, a) ? b : a; }
 
 // Reduces (dtc, dth) over the block; the last block of the grid reduces the
 // per-block results into ctl->dtcourant/dthydro, merges error flags and, if

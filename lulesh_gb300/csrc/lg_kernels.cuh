@@ -110,7 +110,7 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
     // CalcHourglassControlForElems (995-1057)
     const double vk = s.v[k];
     const double determ = s.volo[k] * vk;
-    if (vk <= 0.0) raise_status(ctl, -1);  // lulesh.cc:1034-1040
+    if (dle(vk, 0.0)) raise_status(ctl, -1);  // lulesh.cc:1034-1040
     if (!(hourg > 0.)) return;
 
     // CalcFBHourglassForceForElems (710-991), CalcElemFBHourglassForce (667-706)
@@ -340,7 +340,7 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
         const double dzz = -inv_detJ * (bz[0] * Ez[0] + bz[1] * Ez[2] + bz[2] * Ez[3] + bz[3] * Ez[1]);
         s.vdov[k] = dxx + dyy + dzz;
     }
-    if (relativeVolume <= 0.0) raise_status(ctl, -1);  // lulesh.cc:1598-1605
+    if (dle(relativeVolume, 0.0)) raise_status(ctl, -1);  // lulesh.cc:1598-1605
 
     // CalcMonotonicQGradientsForElems
     double g[6];
@@ -367,7 +367,7 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
                                        bz[2] * (zv[2] - zv[4]) + bz[3] * (zv[3] - zv[5]));
         s.vdov[k] = dxx + dyy + dzz;
     }
-    if (relativeVolume <= 0.0) raise_status(ctl, -1);  // lulesh.cc:1598-1605
+    if (dle(relativeVolume, 0.0)) raise_status(ctl, -1);  // lulesh.cc:1598-1605
 
     // CalcMonotonicQGradientsForElems
     double g[6];
