@@ -98,6 +98,11 @@ __device__ __forceinline__ long long dkey(double v)
     return (b ^ (sgn & 0x7fffffffffffffffLL)) - sgn;
 }
 __device__ __forceinline__ bool dlt(double a, double b) { return dkey(a) < dkey(b); }
+// a + 0.0 for a not NaN: a, except -0 -> +0
+__device__ __forceinline__ double plus_zero(double a)
+{
+    return __double_as_longlong(a) == (long long)0x8000000000000000ULL ? 0.0 : a;
+}
 __device__ __forceinline__ bool dle(double a, double b) { return dkey(a) <= dkey(b); }
 // |a| < b for b >= +0: the magnitude bits order like the magnitudes
 __device__ __forceinline__ bool dabs_lt(double a, double b)
@@ -249,9 +254,10 @@ __device__ __forceinline__ EosOut eos_reps_rho(const Params &P, double e_in, dou
             compression = 0.;
             compHalfStep = 0.;
         }
-        const double work = 0.;
-
-        e_new = e_old - .5 * delvc * (p_old + q_old) + .5 * work;
+        // The reference adds .5 * work with work = 0 (lulesh.cc:2065, 2103, 2286):
+        // x + 0.0 is x except that -0 becomes +0, which plus_zero does on the
+        // integer pipe.
+        e_new = plus_zero(e_old - .5 * delvc * (p_old + q_old));
         if (M::lt(e_new, P.emin)) e_new = P.emin;
 
         const double pHalfStep = pressure<M>(P, bvc, pbvc, e_new, compHalfStep, vc);
@@ -264,7 +270,7 @@ __device__ __forceinline__ EosOut eos_reps_rho(const Params &P, double e_in, dou
         }
         e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (pHalfStep + q_new));
 
-        e_new += .5 * work;
+        e_new = plus_zero(e_new);
         if (M::abs_lt(e_new, P.e_cut)) e_new = 0.;
         if (M::lt(e_new, P.emin)) e_new = P.emin;
 
