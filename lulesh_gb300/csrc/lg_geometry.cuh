@@ -4,10 +4,10 @@
 // the reference scales by powers of two, some functions apply the product of
 // those factors once (each says so); a power of two scales a rounded result
 // exactly, so with R = double and no contraction the values are the
-// reference's bit for bit.  node_normals_nozero, node_normals_x8,
-// area_face_cross (through char_length<R, true>) and hourglass_modes are
-// algebraically equal reformulations that round differently; only the FMA
-// build uses them.
+// reference's bit for bit.  node_normals_x8, area_face_cross (through
+// char_length<R, true>), body_diagonals / diag_directions /
+// monoq_gradients_diag and hourglass_modes are algebraically equal
+// reformulations that round differently; only the FMA build uses them.
 #pragma once
 
 #ifdef __CUDACC__
@@ -285,36 +285,6 @@ LG_HD void node_normals(R *pfx, R *pfy, R *pfz, const R *x, const R *y,
     face_normal(pfx, pfy, pfz, x, y, z, 4, 7, 6, 5);
 }
 
-// CalcElemNodeNormals with each node's three face areas summed in the
-// reference's face order but starting from the first area instead of from
-// 0.0.  Equal to node_normals except for the sign of an all-zero sum; the
-// FMA build uses it (the strict build keeps node_normals).
-template <typename R>
-LG_HD void node_normals_nozero(R *pfx, R *pfy, R *pfz, const R *x, const R *y, const R *z)
-{
-    R ax[6], ay[6], az[6];
-    constexpr int F[6][4] = {{0, 1, 2, 3}, {0, 4, 5, 1}, {1, 5, 6, 2},
-                             {2, 6, 7, 3}, {3, 7, 4, 0}, {4, 7, 6, 5}};
-#pragma unroll
-    for (int f = 0; f < 6; ++f)
-        face_area(x, y, z, F[f][0], F[f][1], F[f][2], F[f][3], ax[f], ay[f], az[f]);
-    // faces of node n, in face order: 0:{0,1,4} 1:{0,1,2} 2:{0,2,3} 3:{0,3,4}
-    // 4:{1,4,5} 5:{1,2,5} 6:{2,3,5} 7:{3,4,5}
-#define LG_NN(P, A)                                 \
-    P[0] = (A[0] + A[1]) + A[4];                    \
-    P[1] = (A[0] + A[1]) + A[2];                    \
-    P[2] = (A[0] + A[2]) + A[3];                    \
-    P[3] = (A[0] + A[3]) + A[4];                    \
-    P[4] = (A[1] + A[4]) + A[5];                    \
-    P[5] = (A[1] + A[2]) + A[5];                    \
-    P[6] = (A[2] + A[3]) + A[5];                    \
-    P[7] = (A[3] + A[4]) + A[5];
-    LG_NN(pfx, ax)
-    LG_NN(pfy, ay)
-    LG_NN(pfz, az)
-#undef LG_NN
-}
-
 // Body diagonals r6 - r0, r5 - r3, r7 - r1, r4 - r2 of one coordinate.
 template <typename R>
 LG_HD void body_diagonals(const R *a, R D[4])
@@ -380,7 +350,9 @@ LG_HD void monoq_gradients_diag(const R *Dx, const R *Dy, const R *Dz, const R *
 // reference's bisectors of face (a, b, c, d) are (p + q) / 2 and (p - q) / 2
 // for p = r_c - r_a, q = r_d - r_b, so its area vector
 // 0.25 (p + q)/2 x (p - q)/2 equals (q x p) / 8 in exact arithmetic.  Each
-// node sums its three faces' q x p as node_normals_nozero does; the caller
+// node sums its three faces' q x p in the reference's face order, starting
+// from the first face instead of from 0.0 (equal but for the sign of an
+// all-zero sum); the caller
 // applies the factor 1/8 (an exact power of two) once.  12 operations per
 // face instead of 27; the rounding differs from the reference's.
 template <typename R>
