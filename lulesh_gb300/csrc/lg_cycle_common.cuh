@@ -16,6 +16,9 @@ namespace lg {
 namespace LG_NS {
 
 constexpr int kBlock = 128;
+// k_material's block when it runs one item per element (the dt partials are
+// sized for blocks of kBlock, so kMatBlock must not be smaller)
+constexpr int kMatBlock = 256;
 
 // Keeps the compiler from treating a value as loop-invariant, so that every
 // EOS repetition the reference performs is evaluated.
