@@ -602,10 +602,11 @@ def run_gpu(a):
         d.field(f, out=host[f])
     init = {f: host[f].copy() for f in fields}
     h2d = sum(host[f].nbytes for f in fields)
-    # host <-> device copies of a short window vary from run to run (the
-    # download of the 26 fields took 4 to 40 ms in repeated runs at s=150):
-    # the median of three end-to-end runs, each from the initial state
-    reps = 3 if a.steps <= 100 else 1
+    # end-to-end runs of a short window: some runs on a shared host took 37 ms
+    # longer than the others (0.235 s against 0.198 s for 20 cycles at s=150),
+    # a stall not reproduced in isolation: the median of five runs, each from
+    # the initial state
+    reps = 5 if a.steps <= 100 else 1
     times, st2 = [], 0
     for _ in range(reps):
         d.reset()  # the time-step state back to cycle 0 (untimed)
