@@ -76,9 +76,9 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 # (profiles/leapfrog_fp64_s150_counts.md).  The mixed build's counts are from
 # s=192, 16 regions, balance 2, cost 4 at cycle 10.
 FP64_SLOTS_PER_UNIT = {
-    "fp64": {"k_forces": 1273, "k_nodes": 78, "k_kinematics": 700, "k_material": 420},
-    "fp64-fma": {"k_forces": 722, "k_nodes": 72, "k_kinematics": 435, "k_material": 364},
-    "mixed": {"k_forces": 24, "k_nodes": 12, "k_kinematics": 95, "k_material": 571},
+    "fp64": {"k_forces": 1272, "k_nodes": 78, "k_kinematics": 699, "k_material": 391},
+    "fp64-fma": {"k_forces": 721, "k_nodes": 72, "k_kinematics": 434, "k_material": 335},
+    "mixed": {"k_forces": 24, "k_nodes": 12, "k_kinematics": 95, "k_material": 536},
 }
 # The workload (nx, regions, balance, cost) each build's counts were taken
 # with; k_material's depend on the region mix, the others on nothing.
@@ -97,9 +97,9 @@ FP64_LANES_PER_SM_CYCLE = 2.0
 # per-corner force scratch (k_forces writes it, k_nodes reads it) and the
 # region-order gathers of k_material.
 TRAFFIC_PER_UNIT = {
-    "fp64": {"k_forces": 496.6, "k_nodes": 568.3, "k_kinematics": 166.5, "k_material": 292.0},
-    "fp64-fma": {"k_forces": 496.2, "k_nodes": 568.0, "k_kinematics": 166.6, "k_material": 291.5},
-    "mixed": {"k_forces": 219.7, "k_nodes": 277.5, "k_kinematics": 148.4, "k_material": 270.2},
+    "fp64": {"k_forces": 496.1, "k_nodes": 568.2, "k_kinematics": 166.4, "k_material": 291.2},
+    "fp64-fma": {"k_forces": 496.1, "k_nodes": 567.9, "k_kinematics": 166.6, "k_material": 291.5},
+    "mixed": {"k_forces": 219.6, "k_nodes": 277.5, "k_kinematics": 148.4, "k_material": 269.9},
 }
 TRAFFIC_SOURCE = {"fp64": "ncu DRAM bytes of the s=150 benchmark mesh (cycle 10)",
                   "fp64-fma": "ncu DRAM bytes of the s=150 benchmark mesh (cycle 10)",
