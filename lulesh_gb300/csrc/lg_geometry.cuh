@@ -385,6 +385,102 @@ LG_HD void node_normals_x8(R *pfx, R *pfy, R *pfz, const R *x, const R *y, const
 #undef LG_NN
 }
 
+// The twelve differences of CalcElemVolume (lulesh.cc:1274-1356) for one
+// coordinate; they are also the element's twelve face diagonals.  Order:
+// 0 d20, 1 d31, 2 d50, 3 d14, 4 d61, 5 d25, 6 d72, 7 d63, 8 d43, 9 d70,
+// 10 d64, 11 d57 (dab = r_a - r_b).
+template <typename R>
+LG_HD void elem_differences(const R *a, R d[12])
+{
+    d[0] = a[2] - a[0];
+    d[1] = a[3] - a[1];
+    d[2] = a[5] - a[0];
+    d[3] = a[1] - a[4];
+    d[4] = a[6] - a[1];
+    d[5] = a[2] - a[5];
+    d[6] = a[7] - a[2];
+    d[7] = a[6] - a[3];
+    d[8] = a[4] - a[3];
+    d[9] = a[7] - a[0];
+    d[10] = a[6] - a[4];
+    d[11] = a[5] - a[7];
+}
+
+// node_normals_x8 from elem_differences: face (a, b, c, d) has area vector
+// 8 (q x p) with p = r_c - r_a, q = r_d - r_b, which are (up to sign) two of
+// the twelve differences.  The same operations as node_normals_x8.
+template <typename R>
+LG_HD void node_normals_x8_diff(R *pfx, R *pfy, R *pfz, const R *dx, const R *dy, const R *dz)
+{
+    // (q, p) per face; q x p = p x (-q) where q is the negated difference
+    constexpr int Q[6] = {1, 3, 5, 6, 8, 11}, P[6] = {0, 2, 4, 7, 9, 10};
+    R ax[6], ay[6], az[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        const int q = Q[f], p = P[f];
+        ax[f] = dy[q] * dz[p] - dz[q] * dy[p];
+        ay[f] = dz[q] * dx[p] - dx[q] * dz[p];
+        az[f] = dx[q] * dy[p] - dy[q] * dx[p];
+    }
+#define LG_NN(P_, A)                                \
+    P_[0] = (A[0] + A[1]) + A[4];                   \
+    P_[1] = (A[0] + A[1]) + A[2];                   \
+    P_[2] = (A[0] + A[2]) + A[3];                   \
+    P_[3] = (A[0] + A[3]) + A[4];                   \
+    P_[4] = (A[1] + A[4]) + A[5];                   \
+    P_[5] = (A[1] + A[2]) + A[5];                   \
+    P_[6] = (A[2] + A[3]) + A[5];                   \
+    P_[7] = (A[3] + A[4]) + A[5];
+    LG_NN(pfx, ax)
+    LG_NN(pfy, ay)
+    LG_NN(pfz, az)
+#undef LG_NN
+}
+
+// 12 x the volume gradient (CalcElemVolumeDerivative without its 1/12,
+// lulesh.cc:591-663) from elem_differences.  CalcElemVolume is
+// (1/12) sum_k a_k . (b_k x c_k) with (a, b, c) = (d31 + d72, d63, d20),
+// (d43 + d57, d64, d70), (d14 + d25, d61, d50); its gradient is, per node,
+// a signed sum of X_k = b_k x c_k, Y_k = c_k x a_k and Z_k = a_k x b_k:
+// nine cross products where the reference's VoluDer forms 24.  Equal to
+// volume_derivative<R, false> in exact arithmetic; the rounding differs.
+template <typename R>
+LG_HD void volume_gradient_x12_diff(const R *dx, const R *dy, const R *dz, R *gx, R *gy, R *gz)
+{
+    const R a1x = dx[1] + dx[6], a1y = dy[1] + dy[6], a1z = dz[1] + dz[6];
+    const R a2x = dx[8] + dx[11], a2y = dy[8] + dy[11], a2z = dz[8] + dz[11];
+    const R a3x = dx[3] + dx[5], a3y = dy[3] + dy[5], a3z = dz[3] + dz[5];
+#define LG_CR(N, ux, uy, uz, vx, vy, vz)                                             \
+    const R N##x = (uy) * (vz) - (uz) * (vy), N##y = (uz) * (vx) - (ux) * (vz),      \
+            N##z = (ux) * (vy) - (uy) * (vx);
+    // k = 1: b = d63 (7), c = d20 (0)
+    LG_CR(X1, dx[7], dy[7], dz[7], dx[0], dy[0], dz[0])
+    LG_CR(Y1, dx[0], dy[0], dz[0], a1x, a1y, a1z)
+    LG_CR(Z1, a1x, a1y, a1z, dx[7], dy[7], dz[7])
+    // k = 2: b = d64 (10), c = d70 (9)
+    LG_CR(X2, dx[10], dy[10], dz[10], dx[9], dy[9], dz[9])
+    LG_CR(Y2, dx[9], dy[9], dz[9], a2x, a2y, a2z)
+    LG_CR(Z2, a2x, a2y, a2z, dx[10], dy[10], dz[10])
+    // k = 3: b = d61 (4), c = d50 (2)
+    LG_CR(X3, dx[4], dy[4], dz[4], dx[2], dy[2], dz[2])
+    LG_CR(Y3, dx[2], dy[2], dz[2], a3x, a3y, a3z)
+    LG_CR(Z3, a3x, a3y, a3z, dx[4], dy[4], dz[4])
+#undef LG_CR
+#define LG_G(C)                                     \
+    g##C[0] = -Z1##C - Z2##C - Z3##C;               \
+    g##C[1] = -X1##C + X3##C - Y3##C;               \
+    g##C[2] = -X1##C + Z1##C + X3##C;               \
+    g##C[3] = X1##C - Y1##C - X2##C;                \
+    g##C[4] = X2##C - Y2##C - X3##C;                \
+    g##C[5] = X2##C - X3##C + Z3##C;                \
+    g##C[6] = Y1##C + Y2##C + Y3##C;                \
+    g##C[7] = X1##C - X2##C + Z2##C;
+    LG_G(x)
+    LG_G(y)
+    LG_G(z)
+#undef LG_G
+}
+
 // The four hourglass mode sums sum_k gam(m, k) * v[k] of CalcFBHourglassForceForElems
 // (lulesh.cc:894-920) by a pairwise butterfly: 18 additions instead of 28.
 // The FMA build uses it; it rounds differently from the left-to-right sums.

@@ -73,6 +73,9 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
     int nd[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) nd[j] = __ldg(&s.nodelistT[(size_t)j * E + k]);
+#if LG_REASSOC
+    double gvx[8], gvy[8], gvz[8];  // 12 x the volume gradient (hourglass part)
+#endif
     double x[8], y[8], z[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
@@ -85,9 +88,18 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
     {
         double pfx[8], pfy[8], pfz[8];
 #if LG_REASSOC
-        // 8 x the normals; the 1/8 goes into sig (exact)
+        // 8 x the normals from the twelve differences, which also give the
+        // volume gradient of the hourglass part below; the 1/8 goes into sig
+        // (exact)
         const double sig = (-s.p[k] - s.q[k]) * 0.125;
-        node_normals_x8(pfx, pfy, pfz, x, y, z);
+        {
+            double dX[12], dY[12], dZ[12];
+            elem_differences(x, dX);
+            elem_differences(y, dY);
+            elem_differences(z, dZ);
+            node_normals_x8_diff(pfx, pfy, pfz, dX, dY, dZ);
+            volume_gradient_x12_diff(dX, dY, dZ, gvx, gvy, gvz);
+        }
 #else
         const double sig = -s.p[k] - s.q[k];
         node_normals(pfx, pfy, pfz, x, y, z);
@@ -117,9 +129,9 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
     double hourgam[8][4];
 #if LG_REASSOC
     {
-        // 12 x dV/dx, with 1/(12 volume) folded into the four mode sums
-        double dvdx[8], dvdy[8], dvdz[8];
-        volume_derivative<double, false>(x, y, z, dvdx, dvdy, dvdz);
+        // 12 x dV/dx (from the twelve differences, above), with 1/(12 volume)
+        // folded into the four mode sums
+        const double *dvdx = gvx, *dvdy = gvy, *dvdz = gvz;
         const double volinv12 = (1.0 / determ) * (1.0 / 12.0);
         double hmx[4], hmy[4], hmz[4];
         hourglass_modes(x, hmx);

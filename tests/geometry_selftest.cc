@@ -115,6 +115,33 @@ int main(int argc, char **argv)
         near("char_length from diagonals", cl, char_length<double, true>(x, y, z, vol),
              1e-12 * std::fabs(cl));
 
+        // the normals from the twelve differences are node_normals_x8's
+        // operations; the volume gradient from them is the reference's
+        // CalcElemVolumeDerivative within its rounding
+        {
+            double dX[12], dY[12], dZ[12], qx[8], qy[8], qz[8];
+            elem_differences(x, dX);
+            elem_differences(y, dY);
+            elem_differences(z, dZ);
+            node_normals_x8(px, py, pz, x, y, z);
+            node_normals_x8_diff(qx, qy, qz, dX, dY, dZ);
+            for (int j = 0; j < 8; ++j) {
+                check("normals from the differences x", px[j], qx[j]);
+                check("normals from the differences y", py[j], qy[j]);
+                check("normals from the differences z", pz[j], qz[j]);
+            }
+            geo_ref_volume_derivative(x, y, z, rx, ry, rz);
+            volume_gradient_x12_diff(dX, dY, dZ, qx, qy, qz);
+            // VoluDer multiplies sums of absolute coordinates (size |r|^2)
+            // that cancel to a result of size h^2: its own error is ~eps |r|^2
+            const double tol_v = 64 * 2.220446049250313e-16 * omax * omax;
+            for (int j = 0; j < 8; ++j) {
+                near("volume gradient x", rx[j], qx[j] / 12.0, tol_v);
+                near("volume gradient y", ry[j], qy[j] / 12.0, tol_v);
+                near("volume gradient z", rz[j], qz[j] / 12.0, tol_v);
+            }
+        }
+
         // the velocity gradient from the body diagonals (at dt = 0 the
         // half-step diagonals are the coordinates' own)
         double Dx[4], Dy[4], Dz[4], Ex[4], Ey[4], Ez[4];
