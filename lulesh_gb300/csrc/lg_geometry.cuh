@@ -285,6 +285,26 @@ LG_HD void node_normals(R *pfx, R *pfy, R *pfz, const R *x, const R *y,
     face_normal(pfx, pfy, pfz, x, y, z, 4, 7, 6, 5);
 }
 
+// 1 / sqrt(a): the device's reciprocal square root (within an ulp or two;
+// not the correctly rounded 1 / sqrt(a), so only the FMA build's
+// reformulated forms use it), the quotient on the host.
+LG_HD double rsqrt_fast(double a)
+{
+#ifdef __CUDA_ARCH__
+    return rsqrt(a);
+#else
+    return 1.0 / sqrt(a);
+#endif
+}
+LG_HD float rsqrt_fast(float a)
+{
+#ifdef __CUDA_ARCH__
+    return rsqrtf(a);
+#else
+    return 1.0f / sqrtf(a);
+#endif
+}
+
 // Body diagonals r6 - r0, r5 - r3, r7 - r1, r4 - r2 of one coordinate.
 template <typename R>
 LG_HD void body_diagonals(const R *a, R D[4])
@@ -328,22 +348,24 @@ LG_HD void monoq_gradients_diag(const R *Dx, const R *Dy, const R *Dz, const R *
     diag_directions(Ex, vxi, vxj, vxk);
     diag_directions(Ey, vyi, vyj, vyk);
     diag_directions(Ez, vzi, vzj, vzk);
+    // vol / sqrt(|a|^2) by the reciprocal square root, and norm applied to
+    // the dot product once
     R ax, ay, az;
     ax = dyi * dzj - dzi * dyj;
     ay = dzi * dxj - dxi * dzj;
     az = dxi * dyj - dyi * dxj;
-    out[2] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
-    out[5] = (ax * norm) * vxk + (ay * norm) * vyk + (az * norm) * vzk;
+    out[2] = vol_s * rsqrt_fast(ax * ax + ay * ay + az * az + ptiny_s);
+    out[5] = norm * (ax * vxk + ay * vyk + az * vzk);
     ax = dyj * dzk - dzj * dyk;
     ay = dzj * dxk - dxj * dzk;
     az = dxj * dyk - dyj * dxk;
-    out[0] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
-    out[3] = (ax * norm) * vxi + (ay * norm) * vyi + (az * norm) * vzi;
+    out[0] = vol_s * rsqrt_fast(ax * ax + ay * ay + az * az + ptiny_s);
+    out[3] = norm * (ax * vxi + ay * vyi + az * vzi);
     ax = dyk * dzi - dzk * dyi;
     ay = dzk * dxi - dxk * dzi;
     az = dxk * dyi - dyk * dxi;
-    out[1] = vol_s / sqrt(ax * ax + ay * ay + az * az + ptiny_s);
-    out[4] = (ax * norm) * vxj + (ay * norm) * vyj + (az * norm) * vzj;
+    out[1] = vol_s * rsqrt_fast(ax * ax + ay * ay + az * az + ptiny_s);
+    out[4] = norm * (ax * vxj + ay * vyj + az * vzj);
 }
 
 // 8 x the node normals of CalcElemNodeNormals from the faces' diagonals: the
@@ -596,8 +618,8 @@ LG_HD R area_face_cross(const R *x, const R *y, const R *z, int a, int b, int c,
 // CalcElemCharacteristicLength, lulesh.cc:1394-1435 (std::max(a,b) is
 // (a < b) ? b : a).  kCross (the FMA build) takes the face areas from
 // area_face_cross: the maximum of a quarter of each area, and
-// 4 v / sqrt(4 m) = 2 v / sqrt(m) exactly, since the factor 4 only shifts
-// exponents.
+// 4 v / sqrt(4 m) = 2 v / sqrt(m), the factor 4 only shifting exponents,
+// evaluated as 2 v rsqrt(m).
 template <typename R, bool kCross = false>
 LG_HD R char_length(const R *x, const R *y, const R *z, R volume)
 {
@@ -609,7 +631,7 @@ LG_HD R char_length(const R *x, const R *y, const R *z, R volume)
         a = area_face_cross(x, y, z, 1, 2, 6, 5); m = lt(a, m) ? m : a;
         a = area_face_cross(x, y, z, 2, 3, 7, 6); m = lt(a, m) ? m : a;
         a = area_face_cross(x, y, z, 3, 0, 4, 7); m = lt(a, m) ? m : a;
-        return R(2.0) * volume / sqrt(m);
+        return R(2.0) * volume * rsqrt_fast(m);
     }
     R cl = R(0.0), a;
     a = area_face(x, y, z, 0, 1, 2, 3); cl = lt(a, cl) ? cl : a;
