@@ -72,12 +72,13 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 # or not, since a warp instruction holds the pipe for the same time either
 # way) x 32 / units (elements; k_nodes: nodes), from ncu captures of the four
 # cycle kernels of the benchmark problem (s=150, 11 regions, balance 1, cost
-# 1) at cycle 10; captures at cycles 1 to 500 agree to 0.7 %
-# (profiles/leapfrog_fp64_s150_counts.md).  The mixed build's counts are from
-# s=192, 16 regions, balance 2, cost 4 at cycle 10.
+# 1) at cycle 10; captures of the same kernels at cycles 1 to 500 agreed to
+# 0.8 %, since the elements the blast has reached stay a small share of the
+# mesh.  The mixed build's counts are from s=192, 16 regions, balance 2,
+# cost 4 at cycle 10.
 FP64_SLOTS_PER_UNIT = {
-    "fp64": {"k_forces": 1272, "k_nodes": 78, "k_kinematics": 699, "k_material": 391},
-    "fp64-fma": {"k_forces": 721, "k_nodes": 72, "k_kinematics": 434, "k_material": 335},
+    "fp64": {"k_forces": 1272, "k_nodes": 78.5, "k_kinematics": 699, "k_material": 391},
+    "fp64-fma": {"k_forces": 664, "k_nodes": 72.5, "k_kinematics": 388, "k_material": 335},
     "mixed": {"k_forces": 24, "k_nodes": 12, "k_kinematics": 95, "k_material": 536},
 }
 # The workload (nx, regions, balance, cost) each build's counts were taken
@@ -98,7 +99,7 @@ FP64_LANES_PER_SM_CYCLE = 2.0
 # region-order gathers of k_material.
 TRAFFIC_PER_UNIT = {
     "fp64": {"k_forces": 496.1, "k_nodes": 568.2, "k_kinematics": 166.4, "k_material": 291.2},
-    "fp64-fma": {"k_forces": 496.1, "k_nodes": 567.9, "k_kinematics": 166.6, "k_material": 291.5},
+    "fp64-fma": {"k_forces": 496.5, "k_nodes": 568.0, "k_kinematics": 165.9, "k_material": 291.2},
     "mixed": {"k_forces": 219.6, "k_nodes": 277.5, "k_kinematics": 148.4, "k_material": 269.9},
 }
 TRAFFIC_SOURCE = {"fp64": "ncu DRAM bytes of the s=150 benchmark mesh (cycle 10)",
@@ -608,6 +609,7 @@ def run_gpu(a):
     # the initial state
     reps = 5 if a.steps <= 100 else 1
     times, st2 = [], 0
+    phases = {"h2d": [], "cycles": [], "d2h": []}  # host clock, per run
     for _ in range(reps):
         d.reset()  # the time-step state back to cycle 0 (untimed)
         for f in fields:
@@ -616,15 +618,20 @@ def run_gpu(a):
         t0 = time.perf_counter()
         for f in fields:
             d.set_field(f, host[f])
+        t1 = time.perf_counter()
         st2 = d.step(a.steps) or st2
+        t2 = time.perf_counter()
         for f in fields:
             d.field(f, out=host[f])
-        times.append(time.perf_counter() - t0)
+        t3 = time.perf_counter()
+        times.append(t3 - t0)
+        for k, v in zip(phases, (t1 - t0, t2 - t1, t3 - t2)):
+            phases[k].append(round(v, 5))
         _barrier(dist)
     t_e2e = _max_over_ranks(dist, statistics.median(times))
     e2e = {"value": ws * E * a.steps / (t_e2e * 1e6), "unit": UNIT,
            "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": h2d / a.steps,
-           "status": st2, "runs": reps, "run_seconds": times}
+           "status": st2, "runs": reps, "run_seconds": times, "phase_seconds": phases}
 
     # the same when the caller keeps the reference's Domain on the host and
     # syncs it around every cycle (the second binding of the integration
