@@ -6,7 +6,8 @@
 // exactly, so with R = double and no contraction the values are the
 // reference's bit for bit.  node_normals_x8, area_face_cross (through
 // char_length<R, true>), body_diagonals / diag_directions /
-// monoq_gradients_diag and hourglass_modes are algebraically equal
+// monoq_gradients_diag / monoq_gradients_dirs / velocity_trace_dirs and
+// hourglass_modes are algebraically equal
 // reformulations that round differently; only the FMA build uses them.
 #pragma once
 
@@ -331,23 +332,21 @@ LG_HD void diag_directions(const R D[4], R &xi, R &et, R &ze)
     ze = s + t;
 }
 
-// CalcMonotonicQGradientsForElems for one element from the body diagonals of
-// its coordinates (Dx, Dy, Dz) and velocities (Ex, Ey, Ez), with the powers of
-// two folded as in monoq_gradients<R, true>.
+// CalcMonotonicQGradientsForElems for one element from the xi, eta and zeta
+// differences of its coordinates (P) and velocities (V), 4 x the reference's
+// (diag_directions of the body diagonals; P[3c..3c+2] and V[3c..3c+2] are
+// coordinate c's xi, eta, zeta), with the powers of two folded as in
+// monoq_gradients<R, true>.
 template <typename R>
-LG_HD void monoq_gradients_diag(const R *Dx, const R *Dy, const R *Dz, const R *Ex, const R *Ey,
-                                const R *Ez, R vol, R out[6])
+LG_HD void monoq_gradients_dirs(const R P[9], const R V[9], R vol, R out[6])
 {
     const R ptiny_s = R(256.e-36);
     const R norm = (R(1.0) / (vol + R(1.e-36))) * R(0.015625);
     const R vol_s = R(16.0) * vol;
-    R dxi, dxj, dxk, dyi, dyj, dyk, dzi, dzj, dzk, vxi, vxj, vxk, vyi, vyj, vyk, vzi, vzj, vzk;
-    diag_directions(Dx, dxi, dxj, dxk);
-    diag_directions(Dy, dyi, dyj, dyk);
-    diag_directions(Dz, dzi, dzj, dzk);
-    diag_directions(Ex, vxi, vxj, vxk);
-    diag_directions(Ey, vyi, vyj, vyk);
-    diag_directions(Ez, vzi, vzj, vzk);
+    const R dxi = P[0], dxj = P[1], dxk = P[2], dyi = P[3], dyj = P[4], dyk = P[5];
+    const R dzi = P[6], dzj = P[7], dzk = P[8];
+    const R vxi = V[0], vxj = V[1], vxk = V[2], vyi = V[3], vyj = V[4], vyk = V[5];
+    const R vzi = V[6], vzj = V[7], vzk = V[8];
     // vol / sqrt(|a|^2) by the reciprocal square root, and norm applied to
     // the dot product once
     R ax, ay, az;
@@ -366,6 +365,64 @@ LG_HD void monoq_gradients_diag(const R *Dx, const R *Dy, const R *Dz, const R *
     az = dxk * dyi - dyk * dxi;
     out[1] = vol_s * rsqrt_fast(ax * ax + ay * ay + az * az + ptiny_s);
     out[4] = norm * (ax * vxj + ay * vyj + az * vzj);
+}
+
+// The xi, eta, zeta differences of the three coordinates from their body
+// diagonals, in monoq_gradients_dirs' layout.
+template <typename R>
+LG_HD void directions3(const R *Dx, const R *Dy, const R *Dz, R P[9])
+{
+    diag_directions(Dx, P[0], P[1], P[2]);
+    diag_directions(Dy, P[3], P[4], P[5]);
+    diag_directions(Dz, P[6], P[7], P[8]);
+}
+
+// CalcMonotonicQGradientsForElems for one element from the body diagonals of
+// its coordinates (Dx, Dy, Dz) and velocities (Ex, Ey, Ez).
+template <typename R>
+LG_HD void monoq_gradients_diag(const R *Dx, const R *Dy, const R *Dz, const R *Ex, const R *Ey,
+                                const R *Ez, R vol, R out[6])
+{
+    R P[9], V[9];
+    directions3(Dx, Dy, Dz, P);
+    directions3(Ex, Ey, Ez, V);
+    monoq_gradients_dirs(P, V, vol, out);
+}
+
+// dxx + dyy + dzz of CalcElemVelocityGradient (lulesh.cc:1437-1500) with the
+// B matrix and determinant of CalcElemShapeFunctionDerivatives (290-377) at
+// the half-step coordinates x - dt2 v (CalcKinematicsForElems, 1540-1556),
+// from the xi, eta, zeta differences P of the coordinates and V of the
+// velocities (monoq_gradients_dirs' layout):
+// * diag_directions is linear, so 8 x the half-step Jacobian is P - dt2 V;
+// * a row of B is the Jacobian's cofactor row c times the shape functions'
+//   sign pattern, and summed against the velocity differences
+//   v0 - v6, v1 - v7, v2 - v4, v3 - v5 that pattern gives the velocity's own
+//   xi, eta, zeta differences: dxx = (c_x . V_x) / detJ, and so on.
+// The cofactors are 64 x and the determinant 512 x the reference's (which is
+// 8 x det J); the factor 64 cancels in the quotient.  Equal to the
+// reference's trace in exact arithmetic; the rounding differs.
+template <typename R>
+LG_HD R velocity_trace_dirs(const R P[9], const R V[9], R dt2)
+{
+    const R fxi = P[0] - dt2 * V[0], fxe = P[1] - dt2 * V[1], fxz = P[2] - dt2 * V[2];
+    const R fyi = P[3] - dt2 * V[3], fye = P[4] - dt2 * V[4], fyz = P[5] - dt2 * V[5];
+    const R fzi = P[6] - dt2 * V[6], fze = P[7] - dt2 * V[7], fzz = P[8] - dt2 * V[8];
+    const R cxi = (fye * fzz) - (fze * fyz);
+    const R cxe = -(fyi * fzz) + (fzi * fyz);
+    const R cxz = (fyi * fze) - (fzi * fye);
+    const R cyi = -(fxe * fzz) + (fze * fxz);
+    const R cye = (fxi * fzz) - (fzi * fxz);
+    const R cyz = -(fxi * fze) + (fzi * fxe);
+    const R czi = (fxe * fyz) - (fye * fxz);
+    const R cze = -(fxi * fyz) + (fyi * fxz);
+    const R czz = (fxi * fye) - (fyi * fxe);
+    const R det = fxe * cxe + fye * cye + fze * cze;
+    const R tr = (cxi * V[0] + cxe * V[1] + cxz * V[2]) + (cyi * V[3] + cye * V[4] + cyz * V[5]) +
+                 (czi * V[6] + cze * V[7] + czz * V[8]);
+    // the reciprocal, not tr / det: tr is 0 for an element at rest, and a
+    // zero dividend takes the quotient's slow special-operand path
+    return tr * (R(1.0) / det);
 }
 
 // 8 x the node normals of CalcElemNodeNormals from the faces' diagonals: the
@@ -619,16 +676,20 @@ LG_HD R area_face_cross(const R *x, const R *y, const R *z, int a, int b, int c,
 // (a < b) ? b : a).  kCross (the FMA build) takes the face areas from
 // area_face_cross: the maximum of a quarter of each area, and
 // 4 v / sqrt(4 m) = 2 v / sqrt(m), the factor 4 only shifting exponents,
-// evaluated as 2 v rsqrt(m).
+// evaluated as 2 v rsqrt(m).  Three faces are walked in the opposite sense
+// (4,7,6,5 for 4,5,6,7; 0,4,5,1 for 0,1,5,4; 1,5,6,2 for 1,2,6,5), which
+// negates one diagonal and leaves |p x q|^2 unchanged bit for bit: every
+// diagonal is then one of elem_volume's differences with its sign, and
+// the compiler shares them.
 template <typename R, bool kCross = false>
 LG_HD R char_length(const R *x, const R *y, const R *z, R volume)
 {
     if (kCross) {
         R m = R(0.0), a;
         a = area_face_cross(x, y, z, 0, 1, 2, 3); m = lt(a, m) ? m : a;
-        a = area_face_cross(x, y, z, 4, 5, 6, 7); m = lt(a, m) ? m : a;
-        a = area_face_cross(x, y, z, 0, 1, 5, 4); m = lt(a, m) ? m : a;
-        a = area_face_cross(x, y, z, 1, 2, 6, 5); m = lt(a, m) ? m : a;
+        a = area_face_cross(x, y, z, 4, 7, 6, 5); m = lt(a, m) ? m : a;
+        a = area_face_cross(x, y, z, 0, 4, 5, 1); m = lt(a, m) ? m : a;
+        a = area_face_cross(x, y, z, 1, 5, 6, 2); m = lt(a, m) ? m : a;
         a = area_face_cross(x, y, z, 2, 3, 7, 6); m = lt(a, m) ? m : a;
         a = area_face_cross(x, y, z, 3, 0, 4, 7); m = lt(a, m) ? m : a;
         return R(2.0) * volume * rsqrt_fast(m);

@@ -320,43 +320,28 @@ __device__ __forceinline__ void kinematics_element(const DevState &s, const int 
     s.delv[k] = relativeVolume - s.v[k];
     s.arealg[k] = char_length<double, LG_REASSOC != 0>(x, y, z, volume);
 #if LG_REASSOC
-    // The velocity gradient's Jacobian, the half-step coordinates and the
-    // monotonic-Q differences all from the element's body diagonals
-    // (diag_directions): 8 x the Jacobian at x - dt/2 v, the velocity terms
-    // v0 - v6, v1 - v7, v2 - v4, v3 - v5 as -E0, -E2, -E3, -E1.
-    double Dx[4], Dy[4], Dz[4], Ex[4], Ey[4], Ez[4];
-    body_diagonals(x, Dx);
-    body_diagonals(y, Dy);
-    body_diagonals(z, Dz);
-    body_diagonals(xv, Ex);
-    body_diagonals(yv, Ey);
-    body_diagonals(zv, Ez);
+    // The velocity gradient's trace and the monotonic-Q gradients from the
+    // xi, eta, zeta differences of the coordinates (P) and velocities (V),
+    // formed once from the element's body diagonals: the half-step Jacobian
+    // is P - dt/2 V (velocity_trace_dirs).
+    double P[9], V[9];
     {
-        const double dt2 = 0.5 * ctl->deltatime;
-        double Hx[4], Hy[4], Hz[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            Hx[j] = Dx[j] - dt2 * Ex[j];
-            Hy[j] = Dy[j] - dt2 * Ey[j];
-            Hz[j] = Dz[j] - dt2 * Ez[j];
-        }
-        double fxi, fxe, fxz, fyi, fye, fyz, fzi, fze, fzz;
-        diag_directions(Hx, fxi, fxe, fxz);
-        diag_directions(Hy, fyi, fye, fyz);
-        diag_directions(Hz, fzi, fze, fzz);
-        double bx[4], by[4], bz[4];
-        const double inv_detJ =
-            1.0 / shape_derivs_x64_jac(fxi, fxe, fxz, fyi, fye, fyz, fzi, fze, fzz, bx, by, bz);
-        const double dxx = -inv_detJ * (bx[0] * Ex[0] + bx[1] * Ex[2] + bx[2] * Ex[3] + bx[3] * Ex[1]);
-        const double dyy = -inv_detJ * (by[0] * Ey[0] + by[1] * Ey[2] + by[2] * Ey[3] + by[3] * Ey[1]);
-        const double dzz = -inv_detJ * (bz[0] * Ez[0] + bz[1] * Ez[2] + bz[2] * Ez[3] + bz[3] * Ez[1]);
-        s.vdov[k] = dxx + dyy + dzz;
+        double Dx[4], Dy[4], Dz[4];
+        body_diagonals(x, Dx);
+        body_diagonals(y, Dy);
+        body_diagonals(z, Dz);
+        directions3(Dx, Dy, Dz, P);
+        body_diagonals(xv, Dx);
+        body_diagonals(yv, Dy);
+        body_diagonals(zv, Dz);
+        directions3(Dx, Dy, Dz, V);
     }
+    s.vdov[k] = velocity_trace_dirs(P, V, 0.5 * ctl->deltatime);
     if (dle(relativeVolume, 0.0)) raise_status(ctl, -1);  // lulesh.cc:1598-1605
 
     // CalcMonotonicQGradientsForElems
     double g[6];
-    monoq_gradients_diag(Dx, Dy, Dz, Ex, Ey, Ez, volo * relativeVolume, g);
+    monoq_gradients_dirs(P, V, volo * relativeVolume, g);
 #else
     {
         const double dt2 = 0.5 * ctl->deltatime;

@@ -166,6 +166,27 @@ int main(int argc, char **argv)
         near("dzz from diagonals", grad(inv, b + 16, zv),
              -invd * (bz[0] * Ez[0] + bz[1] * Ez[2] + bz[2] * Ez[3] + bz[3] * Ez[1]), tol_g);
 
+        // the trace from the xi, eta, zeta differences at a half step
+        // x - dt2 v (the velocities are O(1), so the step moves a node by up
+        // to 5 % of h), against the reference's B matrix at those coordinates
+        {
+            const double dt2 = 0.05 * h * std::fabs(u(g));
+            double xh[8], yh[8], zh[8], bh[24], deth;
+            for (int j = 0; j < 8; ++j) {
+                xh[j] = x[j] - dt2 * xv[j];
+                yh[j] = y[j] - dt2 * yv[j];
+                zh[j] = z[j] - dt2 * zv[j];
+            }
+            geo_ref_shape(xh, yh, zh, bh, &deth);
+            const double invh = 1.0 / deth;
+            const double tr_ref = grad(invh, bh, xv) + grad(invh, bh + 8, yv) + grad(invh, bh + 16, zv);
+            double P[9], V[9];
+            directions3(Dx, Dy, Dz, P);
+            directions3(Ex, Ey, Ez, V);
+            near("velocity trace from directions", tr_ref, velocity_trace_dirs(P, V, dt2),
+                 3 * tol_g);
+        }
+
         // the monotonic-Q gradients from the body diagonals
         double gref[6], gdia[6];
         monoq_gradients<double, false>(x, y, z, xv, yv, zv, vol, gref);
