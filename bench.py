@@ -603,11 +603,11 @@ def run_gpu(a):
         d.field(f, out=host[f])
     init = {f: host[f].copy() for f in fields}
     h2d = sum(host[f].nbytes for f in fields)
-    # end-to-end runs of a short window: some runs on a shared host took 37 ms
-    # longer than the others (0.235 s against 0.198 s for 20 cycles at s=150),
-    # a stall not reproduced in isolation: the median of five runs, each from
-    # the initial state
-    reps = 5 if a.steps <= 100 else 1
+    # the median of several end-to-end runs, each from the initial state: on
+    # a shared host some uploads or downloads of the 709 MB took 25-90 ms
+    # instead of 4 (phase_seconds shows which), a stall not seen on a fresh
+    # host
+    reps = 5 if a.steps <= 100 else 3
     times, st2 = [], 0
     phases = {"h2d": [], "cycles": [], "d2h": []}  # host clock, per run
     for _ in range(reps):
