@@ -172,8 +172,14 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
 #endif
     const double ss1 = s.ss[k];
     const double mass1 = s.elemMass[k];
+#if LG_REASSOC
+    // the reciprocal cube root in place of cbrt and a quotient; the
+    // coefficient goes into the four mode sums hxx (4 products, not 8)
+    const double coefficient = (-hourg * 0.01 * ss1 * mass1) * rcbrt(determ);
+#else
     const double volume13 = cbrt(determ);
     const double coefficient = -hourg * 0.01 * ss1 * mass1 / volume13;
+#endif
     const double *vel[3] = {s.xd, s.yd, s.zd};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -186,11 +192,21 @@ __device__ __forceinline__ void forces_element(const DevState &s, const int k, C
             hxx[i] = hourgam[0][i] * u[0] + hourgam[1][i] * u[1] + hourgam[2][i] * u[2] +
                      hourgam[3][i] * u[3] + hourgam[4][i] * u[4] + hourgam[5][i] * u[5] +
                      hourgam[6][i] * u[6] + hourgam[7][i] * u[7];
+#if LG_REASSOC
+#pragma unroll
+        for (int i = 0; i < 4; i++) hxx[i] *= coefficient;
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            cs[(3 + c) * E8 + (size_t)i * E + k] =
+                hourgam[i][0] * hxx[0] + hourgam[i][1] * hxx[1] + hourgam[i][2] * hxx[2] +
+                hourgam[i][3] * hxx[3];
+#else
 #pragma unroll
         for (int i = 0; i < 8; i++)
             cs[(3 + c) * E8 + (size_t)i * E + k] =
                 coefficient * (hourgam[i][0] * hxx[0] + hourgam[i][1] * hxx[1] +
                                hourgam[i][2] * hxx[2] + hourgam[i][3] * hxx[3]);
+#endif
     }
 }
 
