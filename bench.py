@@ -78,7 +78,7 @@ def alg_bytes_per_elem(kernel: str, n_over_e: float) -> float:
 # cost 4 at cycle 10.
 FP64_SLOTS_PER_UNIT = {
     "fp64": {"k_forces": 1272, "k_nodes": 78.5, "k_kinematics": 699, "k_material": 391},
-    "fp64-fma": {"k_forces": 664, "k_nodes": 72.5, "k_kinematics": 333, "k_material": 335},
+    "fp64-fma": {"k_forces": 648, "k_nodes": 72.5, "k_kinematics": 328, "k_material": 335},
     "mixed": {"k_forces": 24, "k_nodes": 12, "k_kinematics": 95, "k_material": 536},
 }
 # The workload (nx, regions, balance, cost) each build's counts were taken
@@ -99,7 +99,7 @@ FP64_LANES_PER_SM_CYCLE = 2.0
 # region-order gathers of k_material.
 TRAFFIC_PER_UNIT = {
     "fp64": {"k_forces": 496.1, "k_nodes": 568.2, "k_kinematics": 166.4, "k_material": 291.2},
-    "fp64-fma": {"k_forces": 496.0, "k_nodes": 568.1, "k_kinematics": 166.1, "k_material": 291.0},
+    "fp64-fma": {"k_forces": 496.1, "k_nodes": 568.1, "k_kinematics": 167.5, "k_material": 291.2},
     "mixed": {"k_forces": 219.6, "k_nodes": 277.5, "k_kinematics": 148.4, "k_material": 269.9},
 }
 TRAFFIC_SOURCE = {"fp64": "ncu DRAM bytes of the s=150 benchmark mesh (cycle 10)",
