@@ -4,11 +4,12 @@
 // the reference scales by powers of two, some functions apply the product of
 // those factors once (each says so); a power of two scales a rounded result
 // exactly, so with R = double and no contraction the values are the
-// reference's bit for bit.  node_normals_x8, area_face_cross (through
+// reference's bit for bit.  node_normals_x8 / node_normals_x8_diff,
+// volume_gradient_x12_diff, area_face_cross and rsqrt_fast (through
 // char_length<R, true>), body_diagonals / diag_directions /
 // monoq_gradients_diag / monoq_gradients_dirs / velocity_trace_dirs and
-// hourglass_modes are algebraically equal
-// reformulations that round differently; only the FMA build uses them.
+// hourglass_modes are algebraically equal reformulations that round
+// differently; only the FMA build uses them.
 #pragma once
 
 #ifdef __CUDACC__

@@ -44,11 +44,17 @@
 #error "define LG_NS"
 #endif
 // LG_REASSOC (the FMA build): algebraically equal forms that save FP64
-// instructions: node normals and face areas from the faces' diagonals
-// (node_normals_x8, area_face_cross), the hourglass_modes butterfly, and the
-// 1/12 and 1/volume factors applied once per mode instead of once per term.
-// The rounding differs from the reference's operand order, as FMA
-// contraction's does; the parity bar covers both.
+// instructions.  k_forces: node normals and the volume gradient from the
+// element's twelve edge differences (node_normals_x8_diff,
+// volume_gradient_x12_diff), the hourglass_modes butterfly, the 1/12 and
+// 1/volume factors applied once per mode, and the hourglass coefficient by
+// the reciprocal cube root applied to the four mode sums.  k_kinematics: face
+// areas from the faces' diagonals (area_face_cross), the velocity-gradient
+// trace and the monotonic-Q gradients from the xi/eta/zeta differences of
+// the coordinates and velocities (velocity_trace_dirs, monoq_gradients_dirs),
+// lengths by reciprocal square roots.  The rounding differs from the
+// reference's operand order, as FMA contraction's does; the parity bar
+// covers both.
 #ifndef LG_REASSOC
 #define LG_REASSOC 0
 #endif
