@@ -24,11 +24,13 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_folded_geometry_equals_oracle_bitwise(tmp_path):
+@pytest.fixture(scope="module")
+def geometry_selftest(tmp_path_factory):
     if not shutil.which("g++") or not shutil.which("gcc"):
         pytest.skip("no host compilers")
-    shim = tmp_path / "shim.o"
-    exe = tmp_path / "geometry_selftest"
+    tmp = tmp_path_factory.mktemp("geometry")
+    shim = tmp / "shim.o"
+    exe = tmp / "geometry_selftest"
     subprocess.run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-I", os.path.join(ROOT, "oracle"),
                     "-c", os.path.join(ROOT, "tests", "geometry_ref_shim.c"), "-o", str(shim)],
                    check=True)
@@ -36,9 +38,35 @@ def test_folded_geometry_equals_oracle_bitwise(tmp_path):
                     "-I", os.path.join(ROOT, "lulesh_gb300", "csrc"), "-I", os.path.join(ROOT, "oracle"),
                     os.path.join(ROOT, "tests", "geometry_selftest.cc"), str(shim), "-lm",
                     "-o", str(exe)], check=True)
-    r = subprocess.run([str(exe), "100000"], capture_output=True, text=True)
+    return str(exe)
+
+
+def test_folded_geometry_equals_oracle_bitwise(geometry_selftest):
+    r = subprocess.run([geometry_selftest, "100000"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout[-2000:]
     assert r.stdout.strip().endswith("mismatches 0"), r.stdout[-2000:]
+
+
+# every reassociated form the FMA build uses, by the label of its check
+REASSOCIATED = ["normal x from diagonals", "normal y from diagonals", "normal z from diagonals",
+                "char_length from diagonals", "volume gradient x", "volume gradient y",
+                "volume gradient z", "dxx from diagonals", "dyy from diagonals",
+                "dzz from diagonals", "velocity trace from directions", "delx from diagonals",
+                "delv from diagonals"]
+
+
+def test_reassociated_tolerances_see_a_planted_error(geometry_selftest):
+    """The oracle's values scaled by 1 + 1e-8 (plant mode): each reassociated
+    form's tolerance is tight enough that its check reports elements beyond it."""
+    r = subprocess.run([geometry_selftest, "20000", "plant"], capture_output=True, text=True)
+    assert r.returncode == 1, r.stdout[-2000:]
+    tripped = {}
+    for line in r.stdout.splitlines():
+        if line.startswith("planted "):
+            label, rest = line[len("planted "):].rsplit(": ", 1)
+            tripped[label] = int(rest.split()[0])
+    for label in REASSOCIATED:
+        assert tripped.get(label, 0) > 0, (label, tripped)
 
 
 def _dkey(v: np.ndarray) -> np.ndarray:
